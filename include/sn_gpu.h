@@ -1,0 +1,230 @@
+/*
+ * sn_gpu.h -- C ABI of the GB300 Metropolis dipole-lattice sweep.
+ *
+ * Drop-in boundary for the StarryNight hot loop.  The reference has no
+ * library API: its sweep is MC_moves(MCMinorSteps) (src/starrynight-main.c:222,
+ * :248) acting on global state -- the lattice `struct dipole ***lattice`
+ * (src/starrynight-config.c:32-36), the neighbour list (src/starrynight-
+ * montecarlo-core.c:29-36), beta/Efield/CageStrain/K/ConstrainToX
+ * (src/starrynight-config.c:62-85) and the ACCEPT/REJECT counters (:26-27).
+ * This ABI replaces that region: the host keeps the reference's config keys
+ * and driver loop and calls these functions instead.
+ *
+ * Conventions
+ *   - Plain C types only; no CUDA or torch types cross the boundary.
+ *   - The caller owns every host buffer; the handle owns all device memory.
+ *   - Every function returns sn_status (SN_OK == 0); none calls exit().
+ *     sn_gpu_last_error() gives a one-line reason for the last failure.
+ *   - One handle is driven by one host thread; its work runs on the handle's
+ *     own CUDA stream, in order.
+ *   - Lattice arrays are site-major with z fastest: site (x,y,z) is at
+ *     index (x*Y + y)*Z + z, the element order of the reference's
+ *     lattice[x][y][z].  Dipoles are float triples (x,y,z); lengths are
+ *     floats.  A site of length 0 is a vacancy and holds the zero vector.
+ *   - Temperatures are float Kelvin; beta = 300/T (energies in units of
+ *     k_B * 300 K, src/starrynight-main.c:215).
+ */
+#ifndef SN_GPU_H
+#define SN_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sn_status {
+    SN_OK = 0,
+    SN_ERR_ARG = 1,         /* NULL handle/buffer, index out of range, bad value  */
+    SN_ERR_CONFIG = 2,      /* parameters the model cannot take (cutoff, species) */
+    SN_ERR_SCHEDULE = 3,    /* lattice shape admits no conflict-free block/colour schedule */
+    SN_ERR_CUDA = 4,        /* CUDA runtime error (no device, launch failure, ...) */
+    SN_ERR_NOMEM = 5,       /* device or host allocation failed */
+    SN_ERR_TIMEOUT = 6,     /* a bounded device-side wait ran out */
+    SN_ERR_UNSUPPORTED = 7  /* valid request outside what this build implements */
+} sn_status;
+
+#define SN_MAX_SPECIES 10 /* dipoles[10], src/starrynight-config.c:39-43 */
+#define SN_MAX_CUTOFF 6   /* largest DipoleCutOff with a tiled kernel in this build */
+
+/* Model parameters shared by all replicas: the starrynight.cfg keys of the
+ * hot path (src/starrynight-config.c:123-166). */
+typedef struct sn_params {
+    int cutoff;                      /* DipoleCutOff (lattice units)                    */
+    int dim;                         /* 3: sphere proposals; 2: circle (DIM<3 branch)   */
+    int constrain_to_x;              /* ConstrainToX: proposals along +-x,+-y,+-z       */
+    float cage_strain;               /* CageStrain                                      */
+    float K;                         /* K, epitaxial term; applied only when K > 0      */
+    float efield[3];                 /* Efield.{x,y,z}; replicas may override           */
+    int n_species;                   /* length of Dipoles / Prevalence                  */
+    float dipoles[SN_MAX_SPECIES];   /* Dipoles: species lengths (0 = vacancy)          */
+    float prevalence[SN_MAX_SPECIES];/* Prevalence: species probabilities               */
+    uint64_t seed;                   /* default Philox key for replicas with seed 0     */
+} sn_params;
+
+/* One lattice of the replica table (batched mode: many per handle). */
+typedef struct sn_replica_desc {
+    int X, Y, Z;           /* lattice size (reference keys X, Y, Z)        */
+    float T;               /* temperature in Kelvin (reference key T)     */
+    int has_efield;        /* 1: efield below replaces sn_params.efield    */
+    float efield[3];
+    uint64_t seed;         /* Philox key of this replica; 0 -> params.seed + replica */
+} sn_replica_desc;
+
+/* The block/colour schedule chosen for one replica (what the CPU oracle
+ * mirrors).  A sweep visits block colours (cbx,cby,cbz) lexicographically;
+ * inside a block colour it visits site colours (cx,cy,cz) lexicographically;
+ * a site (x,y,z) belongs to block (x/bx, y/by, z/bz) of colour
+ * (block mod m) and to site colour (local coordinate mod s). */
+typedef struct sn_schedule_info {
+    int bx, by, bz;        /* block dimensions                          */
+    int nbx, nby, nbz;     /* blocks per axis                           */
+    int mx, my, mz;        /* block colours per axis                    */
+    int s;                 /* site-colour stride = cutoff + 1           */
+    int halo;              /* halo width = cutoff (0 along z in 2D)     */
+    int tile_slots;        /* shared-memory slots per tile (padded)     */
+    int smem_bytes;        /* dynamic shared memory per block           */
+} sn_schedule_info;
+
+/* Initial lattice patterns (InitialLattice, src/starrynight-main.c:184-203). */
+enum {
+    SN_LATTICE_RANDOM = 0,        /* uniform on the sphere, then solid solution   */
+    SN_LATTICE_FERROELECTRIC = 1  /* all along +x, then solid solution            */
+};
+
+/* Energy precision for sn_gpu_energy / sn_gpu_recompute. */
+enum {
+    SN_ENERGY_FP32 = 0,   /* FP32 local fields, FP64 site products and sums  */
+    SN_ENERGY_FP64 = 1    /* every operation in FP64                          */
+};
+
+typedef struct sn_handle sn_handle;
+
+/* ---- lifecycle --------------------------------------------------------- */
+
+/* Allocates the replica table in HBM, builds the neighbour offsets
+ * (replaces gen_neighbour, src/starrynight-montecarlo-core.c:38-72) and the
+ * per-replica schedule.  Lattices start as all-vacancy until
+ * sn_gpu_init_lattice or sn_gpu_upload_lattice.  Replaces the setup part of
+ * main(), src/starrynight-main.c:153-180. */
+sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_desc *replicas,
+                      sn_handle **out);
+sn_status sn_gpu_destroy(sn_handle *h);
+const char *sn_gpu_status_string(sn_status s);
+const char *sn_gpu_last_error(const sn_handle *h);
+
+/* ---- lattice ----------------------------------------------------------- */
+
+/* Pattern + solid solution on the device from (seed, site) Philox draws.
+ * Replaces initialise_lattice_random/_ferroelectric + solid_solution
+ * (src/starrynight-lattice.c:25-47, :139-171); vacancies get the zero
+ * vector.  seed 0 -> the replica's seed. */
+sn_status sn_gpu_init_lattice(sn_handle *h, int replica, int pattern, uint64_t seed);
+
+/* xyz: 3N floats interleaved; len: N floats or NULL (every site gets
+ * Dipoles[0]).  Sites with len == 0 are stored as zero vectors.  Replaces
+ * the host writes into lattice[x][y][z]. */
+sn_status sn_gpu_upload_lattice(sn_handle *h, int replica, const float *xyz, const float *len);
+/* xyz: 3N floats; len: N floats or NULL.  For the analysis writers that read
+ * lattice[x][y][z] between megasteps (src/starrynight-main.c:51-103). */
+sn_status sn_gpu_download_lattice(sn_handle *h, int replica, float *xyz, float *len);
+
+/* ---- sweep --------------------------------------------------------------- */
+
+/* n_sweeps Metropolis sweeps of every replica (each occupied site attempted
+ * once per sweep), as CUDA-graph launches.  accept/reject (nullable) receive
+ * the totals of this call over all replicas.  Replaces MC_moves(X*Y*Z*n)
+ * (src/starrynight-montecarlo-core.c:143-191) and the ACCEPT/REJECT counters. */
+sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *reject);
+
+/* Total sweeps done so far (the Philox sweep counter). */
+sn_status sn_gpu_sweep_count(const sn_handle *h, uint64_t *sweeps);
+
+/* ---- energies and observables -------------------------------------------- */
+
+/* Full recompute of one replica's energy (FP64 total).  site_E (nullable,
+ * N doubles) receives the site energies e_i = p_i.(len_i h_i - C nn_i + E)
+ * - K(|p_ix|+|p_iy|)[K>0], whose differences are site_energy()'s dE
+ * (src/starrynight-montecarlo-core.c:76-141). */
+sn_status sn_gpu_energy(sn_handle *h, int replica, int precision, double *E_total, double *site_E);
+
+/* Per replica (arrays of n_replicas): E/site and |P|/site from the running
+ * FP64 totals, P = sum_i len_i p_i (P_vec nullable, 3 per replica).  N is
+ * X*Y*Z, as polarisation() divides (src/starrynight-analysis.c:48-62). */
+sn_status sn_gpu_observables(sn_handle *h, double *E_per_site, double *P_abs, double *P_vec);
+
+/* Per-sweep log of one replica since the last call: E/site and |P|/site
+ * after each sweep.  *n_out = entries written (<= max). */
+sn_status sn_gpu_history(sn_handle *h, int replica, int max, double *E_per_site, double *P_abs,
+                         int *n_out);
+
+/* Recompute every replica's energy, compare with the running total, and
+ * restart the running total from the recompute.  *max_rel_drift (nullable)
+ * = max over replicas of |E_running - E_recompute| / max(|E_recompute|, 1). */
+sn_status sn_gpu_recompute(sn_handle *h, int precision, double *max_rel_drift);
+
+/* Make sn_gpu_sweep recompute every `every` sweeps (0 = never) and keep the
+ * largest relative drift seen; read it with sn_gpu_drift. */
+sn_status sn_gpu_set_recompute(sn_handle *h, int every, int precision);
+sn_status sn_gpu_drift(const sn_handle *h, double *max_rel_drift, int *n_checks);
+
+/* ---- run control ---------------------------------------------------------- */
+
+sn_status sn_gpu_set_field(sn_handle *h, int replica, const float efield[3]);
+sn_status sn_gpu_set_temperature(sn_handle *h, int replica, float T);
+sn_status sn_gpu_get_temperature(const sn_handle *h, int replica, float *T);
+
+/* Replica exchange between adjacent temperatures every `every` sweeps
+ * (0 = off); pairs alternate even/odd, swap accepted with probability
+ * min(1, exp((beta_a - beta_b)(E_a - E_b))).  The reference runs independent
+ * temperatures as separate processes (Makefile:48-62); this is the in-GPU
+ * form of that batch. */
+sn_status sn_gpu_set_exchange(sn_handle *h, int every);
+sn_status sn_gpu_exchange_stats(sn_handle *h, uint64_t *attempted, uint64_t *accepted);
+
+/* ---- differentiation ------------------------------------------------------- */
+
+/* Adjoint of the total energy of one replica: dE_dp (nullable, 3N floats) =
+ * dE/dp_i = len_i h_i - C nn_i + E - K(sgn p_ix, sgn p_iy, 0)[K>0] (zero at
+ * vacancies); dE_dparams (nullable, 5 doubles) = dE/d(Dipole, CageStrain,
+ * Ex, Ey, Ez) with dE/dDipole = 2 E_dd / Dipoles[0]; E_total nullable. */
+sn_status sn_gpu_adjoint(sn_handle *h, int replica, float *dE_dp, double *dE_dparams, double *E_total);
+
+/* T=0 projected-gradient descent on the sphere: n_steps of
+ * p <- normalize(p - step (g - (g.p) p)) at every occupied site.  E_trace
+ * (nullable, n_steps+1 doubles) receives E before and after each step. */
+sn_status sn_gpu_quench(sn_handle *h, int replica, int n_steps, float step, double *E_trace);
+
+/* ---- random streams ---------------------------------------------------------- */
+
+/* Philox4x32-10 of n (counter, key) pairs on the device: ctr 4n words,
+ * key 2n words, out 4n words (host buffers).  The stream behind every
+ * proposal, for checking against a CPU restatement. */
+sn_status sn_gpu_philox(const uint32_t *ctr, const uint32_t *key, uint32_t *out, int n);
+/* The proposals the sweep draws in one replica for sites[i] at sweep index
+ * `sweep`: out4[4i..4i+3] = (p'x, p'y, p'z, u); NaN p' when every Marsaglia
+ * try was rejected (the move then keeps the old dipole). */
+sn_status sn_gpu_proposals(const sn_handle *h, int replica, const uint32_t *sites, int n, uint32_t sweep,
+                           float *out4);
+
+/* ---- introspection ---------------------------------------------------------- */
+
+sn_status sn_gpu_schedule(const sn_handle *h, int replica, sn_schedule_info *out);
+/* Host-only: the schedule sn_gpu_init would pick (no GPU needed). */
+sn_status sn_plan_schedule(int X, int Y, int Z, int cutoff, int mixed_lengths, sn_schedule_info *out);
+/* Host-only: 1 if no two sites updated together interact under periodic
+ * boundaries (same block colour and site colour within the cutoff). */
+int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *sched);
+/* Kernel launches issued by this handle so far. */
+sn_status sn_gpu_launch_count(const sn_handle *h, uint64_t *launches);
+/* The handle's CUDA stream as an opaque pointer (for event timing). */
+void *sn_gpu_stream(const sn_handle *h);
+/* Number of neighbour offsets (gen_neighbour's count) for a cutoff. */
+int sn_neighbour_count(int cutoff, int Z);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

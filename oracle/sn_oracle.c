@@ -524,6 +524,9 @@ uint64_t sno_colour_sweep(const sno_model *m, const sno_schedule *sc, const sno_
                                                     if (gpu_after) {
                                                         const float *gx = gpu_after, *gy = gpu_after + N, *gz = gpu_after + 2 * N;
                                                         gacc = (gx[i] != px[i]) || (gy[i] != py[i]) || (gz[i] != pz[i]);
+                                                        /* a proposal equal to the current dipole leaves the
+                                                         * lattice unchanged either way: nothing to compare */
+                                                        if (p[0] == px[i] && p[1] == py[i] && p[2] == pz[i]) gacc = acc;
                                                         if (gacc != acc) {
                                                             if (fabs(margin) <= tol) {
                                                                 if (n_borderline) (*n_borderline)++;

@@ -1,0 +1,1055 @@
+// sn_gpu.cu -- host implementation of the C ABI in include/sn_gpu.h.
+//
+// One handle = one replica table resident in HBM + one CUDA stream.  A sweep
+// is captured once as a CUDA graph (8 block-colour launches of the sweep
+// kernel + the end-of-sweep fold) and replayed; every per-sweep quantity the
+// kernels need (sweep index, temperatures, fields) lives in device memory so
+// the graph never changes.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sn_gpu.h"
+#include "sn_launch.h"
+#include "sn_sweep.cuh"
+
+namespace {
+
+const sn_sweep_launch_fn k_sweep[SN_MAX_CUTOFF + 1] = {nullptr,
+                                                        sn_launch_sweep_rc1,
+                                                        sn_launch_sweep_rc2,
+                                                        sn_launch_sweep_rc3,
+                                                        sn_launch_sweep_rc4,
+                                                        sn_launch_sweep_rc5,
+                                                        sn_launch_sweep_rc6};
+const sn_field_launch_fn k_field[SN_MAX_CUTOFF + 1] = {nullptr,
+                                                        sn_launch_field_rc1,
+                                                        sn_launch_field_rc2,
+                                                        sn_launch_field_rc3,
+                                                        sn_launch_field_rc4,
+                                                        sn_launch_field_rc5,
+                                                        sn_launch_field_rc6};
+const sn_geo_fn k_geo[SN_MAX_CUTOFF + 1] = {nullptr,     sn_geo_rc1, sn_geo_rc2, sn_geo_rc3,
+                                            sn_geo_rc4,  sn_geo_rc5, sn_geo_rc6};
+
+const int kSmemLimit = 227 * 1024;
+
+thread_local std::string g_last_error;
+
+// ---------------------------------------------------------------------------
+// Planner.
+
+int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+void axis_starts(int T, int S, int *start)
+{
+    int acc = 0;
+    for (int k = 0; k < SN_MAX_S; k++) {
+        start[k] = acc;
+        if (k < S && k < T) acc += (T - k + S - 1) / S;
+    }
+}
+
+int pi_host(const int *start, int S, int u) { return start[u % S] + u / S; }
+
+// Sum over site colours and warps of the worst bank multiplicity of the
+// targets' slots (32 lanes -> 32 banks is the ideal: cost 1 per warp).
+long long conflict_cost(const SnTile &t, int S, bool two_d, int Sy, int Sx)
+{
+    long long cost = 0;
+    const int SZ = two_d ? 1 : S;
+    int cnt[32];
+    for (int cx = 0; cx < S; cx++)
+        for (int cy = 0; cy < S; cy++)
+            for (int cz = 0; cz < SZ; cz++) {
+                const int nx = cx < t.B[0] ? ceil_div(t.B[0] - cx, S) : 0;
+                const int ny = cy < t.B[1] ? ceil_div(t.B[1] - cy, S) : 0;
+                const int nz = two_d ? 1 : (cz < t.B[2] ? ceil_div(t.B[2] - cz, S) : 0);
+                const int nt = nx * ny * nz;
+                if (!nt) continue;
+                const int bx0 = pi_host(t.start[0], S, cx + t.H[0]);
+                const int by0 = pi_host(t.start[1], S, cy + t.H[1]);
+                const int bz0 = two_d ? 0 : pi_host(t.start[2], S, cz + t.H[2]);
+                for (int w0 = 0; w0 < nt; w0 += 32) {
+                    memset(cnt, 0, sizeof(cnt));
+                    int worst = 0;
+                    for (int t_ = w0; t_ < std::min(nt, w0 + 32); t_++) {
+                        const int qz = t_ % nz, r = t_ / nz, qy = r % ny, qx = r / ny;
+                        const long long slot = (long long)(bx0 + qx) * Sx + (long long)(by0 + qy) * Sy + bz0 + qz;
+                        const int b = (int)(slot & 31);
+                        worst = std::max(worst, ++cnt[b]);
+                    }
+                    cost += worst;
+                }
+            }
+    return cost;
+}
+
+struct AxisChoice {
+    std::vector<int> cands;
+};
+
+// Candidate block sizes along an axis of length L: L/B even (a 2-colouring
+// of the blocks is then consistent across the periodic boundary) and
+// B >= cutoff (same-colour blocks are then more than cutoff apart).
+std::vector<int> block_candidates(int L, int rc)
+{
+    std::vector<int> c;
+    for (int B = std::max(rc, 1); B <= L / 2; B++)
+        if (L % B == 0 && (L / B) % 2 == 0) c.push_back(B);
+    return c;
+}
+
+bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string &why)
+{
+    if (rc < 1 || rc > SN_MAX_CUTOFF) {
+        why = "cutoff outside 1.." + std::to_string(SN_MAX_CUTOFF);
+        return false;
+    }
+    const bool two_d = (Z == 1);
+    int S, SZ, NS, NF;
+    k_geo[rc](two_d, &S, &SZ, &NS, &NF);
+    const int L[3] = {X, Y, Z};
+    std::vector<int> cands[3];
+    for (int a = 0; a < 3; a++) {
+        if (a == 2 && two_d) {
+            cands[a] = {1};
+            continue;
+        }
+        cands[a] = block_candidates(L[a], rc);
+        if (cands[a].empty()) {
+            why = "axis " + std::string(1, "XYZ"[a]) + "=" + std::to_string(L[a]) +
+                  " has no even number of blocks of at least cutoff=" + std::to_string(rc) + " sites";
+            return false;
+        }
+    }
+    struct Cand {
+        int B[3];
+        long long vol;
+        int balanced;
+    };
+    std::vector<Cand> all;
+    for (int bx : cands[0])
+        for (int by : cands[1])
+            for (int bz : cands[2]) {
+                Cand c{{bx, by, bz}, (long long)bx * by * bz, 0};
+                c.balanced = (bx % S == 0) + (by % S == 0) + (two_d || bz % S == 0);
+                all.push_back(c);
+            }
+    // Largest blocks first (least halo per site), balanced colours first,
+    // then the most cubic.
+    std::sort(all.begin(), all.end(), [](const Cand &a, const Cand &b) {
+        if (a.vol != b.vol) return a.vol > b.vol;
+        if (a.balanced != b.balanced) return a.balanced > b.balanced;
+        const int sa = std::max({a.B[0], a.B[1], a.B[2]}) - std::min({a.B[0], a.B[1], a.B[2]});
+        const int sb = std::max({b.B[0], b.B[1], b.B[2]}) - std::min({b.B[0], b.B[1], b.B[2]});
+        return sa < sb;
+    });
+    for (const Cand &c : all) {
+        SnTile t;
+        memset(&t, 0, sizeof(t));
+        for (int a = 0; a < 3; a++) {
+            t.B[a] = c.B[a];
+            t.H[a] = (a == 2 && two_d) ? 0 : rc;
+            t.T[a] = (a == 2 && two_d) ? 1 : c.B[a] + 2 * rc;
+            t.nb[a] = L[a] / c.B[a];
+            t.m[a] = (a == 2 && two_d) ? 1 : 2;
+            axis_starts(t.T[a], S, t.start[a]);
+        }
+        t.maxt = ceil_div(t.B[0], S) * ceil_div(t.B[1], S) * (two_d ? 1 : ceil_div(t.B[2], S));
+        // quick lower bound on shared memory with no padding
+        {
+            const sn_sweep::Carve cv =
+                sn_sweep::sn_carve(t.T[0] * t.T[1] * t.T[2], t.maxt, S, SZ, NS, NF, mixed);
+            if ((int)cv.total > kSmemLimit) continue;
+        }
+        long long best = -1;
+        int bSy = 0, bSx = 0;
+        for (int dy = 0; dy < 32; dy++) {
+            const int Sy = t.T[2] + dy;
+            for (int dx = 0; dx < 32; dx++) {
+                const int Sx = t.T[1] * Sy + dx;
+                const sn_sweep::Carve cv = sn_sweep::sn_carve(Sx * t.T[0], t.maxt, S, SZ, NS, NF, mixed);
+                if ((int)cv.total > kSmemLimit) continue;
+                const long long cost = conflict_cost(t, S, two_d, Sy, Sx);
+                if (best < 0 || cost < best) {
+                    best = cost;
+                    bSy = Sy;
+                    bSx = Sx;
+                }
+            }
+        }
+        if (best < 0) continue;
+        t.Sy = bSy;
+        t.Sx = bSx;
+        t.slots = bSx * t.T[0];
+        t.smem_bytes = (int)sn_sweep::sn_carve(t.slots, t.maxt, S, SZ, NS, NF, mixed).total;
+        out = t;
+        return true;
+    }
+    why = "no block shape fits in shared memory for this lattice and cutoff";
+    return false;
+}
+
+void fill_info(const SnTile &t, int rc, sn_schedule_info *o)
+{
+    o->bx = t.B[0];
+    o->by = t.B[1];
+    o->bz = t.B[2];
+    o->nbx = t.nb[0];
+    o->nby = t.nb[1];
+    o->nbz = t.nb[2];
+    o->mx = t.m[0];
+    o->my = t.m[1];
+    o->mz = t.m[2];
+    o->s = rc + 1;
+    o->halo = rc;
+    o->tile_slots = t.slots;
+    o->smem_bytes = t.smem_bytes;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct sn_handle {
+    sn_params params{};
+    int nrep = 0;
+    bool mixed = false;
+    float length = 0.0f;   // uniform length
+    float dipole_ref = 0.0f;
+    int rc = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<sn_replica_desc> desc;
+    std::vector<SnTile> tiles;
+    std::vector<SnReplicaDev> reps;
+    // device
+    SnReplicaDev *d_reps = nullptr;
+    SnTile *d_geoms = nullptr;
+    SnAccum *d_acc = nullptr;
+    SnState *d_state = nullptr;
+    uint32_t *d_sweep = nullptr;
+    double *d_hist = nullptr;
+    double *d_red = nullptr;     // 10 per replica
+    double *d_drift = nullptr;   // per replica
+    SnExchange *d_ex = nullptr;
+    int *d_order = nullptr;
+    int *d_flags = nullptr;
+    SnWork *d_work = nullptr;
+    std::vector<int> work_off, work_cnt, work_smem;  // [phase*2 + variant]
+    std::vector<int> fwork_off, fwork_cnt;           // per replica, all blocks
+    std::vector<float *> lattice_mem;
+    // scratch (lazy)
+    float *d_stage = nullptr;
+    size_t stage_floats = 0;
+    double *d_site = nullptr;
+    size_t site_n = 0;
+    float *d_grad = nullptr;
+    size_t grad_n = 0;
+    double *d_trace = nullptr;
+    size_t trace_n = 0;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_nodes = 0;
+    // counters
+    uint64_t launches = 0;
+    uint64_t sweeps = 0;
+    int exchange_every = 0;
+    int recompute_every = 0;
+    int recompute_prec = SN_ENERGY_FP32;
+    int n_checks = 0;
+    std::string err;
+};
+
+namespace {
+
+sn_status fail(sn_handle *h, sn_status s, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    g_last_error = buf;
+    return s;
+}
+
+#define SN_CK(h, x)                                                                                  \
+    do {                                                                                             \
+        cudaError_t e_ = (x);                                                                        \
+        if (e_ != cudaSuccess) return fail((h), SN_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+    } while (0)
+
+sn_status check_rep(sn_handle *h, int r)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    if (r < 0 || r >= h->nrep) return fail(h, SN_ERR_ARG, "replica %d out of range [0,%d)", r, h->nrep);
+    return SN_OK;
+}
+
+sn_status ensure(sn_handle *h, void **p, size_t *have, size_t need, size_t elem)
+{
+    if (*have >= need) return SN_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    cudaError_t e = cudaMalloc(p, need * elem);
+    if (e != cudaSuccess) return fail(h, SN_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", need * elem, cudaGetErrorString(e));
+    *have = need;
+    return SN_OK;
+}
+
+SnFieldArgsHost field_args(sn_handle *h, int r, double *site_e, float *grad, double *red, int stride)
+{
+    SnFieldArgsHost a;
+    a.work = h->d_work + h->fwork_off[r];
+    a.reps = h->d_reps;
+    a.geoms = h->d_geoms;
+    a.cage = h->params.cage_strain;
+    a.K = h->params.K;
+    a.site_e = site_e;
+    a.grad = grad;
+    a.red = red;
+    a.red_stride = stride;
+    return a;
+}
+
+sn_status launch_field(sn_handle *h, int r, bool fp64, const SnFieldArgsHost &a)
+{
+    const bool two_d = h->desc[r].Z == 1;
+    SN_CK(h, k_field[h->rc](fp64, two_d, h->mixed, &a, h->fwork_cnt[r], h->tiles[r].smem_bytes, h->stream));
+    h->launches++;
+    return SN_OK;
+}
+
+// Recompute replica r's running E and P from a full field pass.
+sn_status recompute_one(sn_handle *h, int r, int prec, int record)
+{
+    double *red = h->d_red + 10 * r;
+    SN_CK(h, cudaMemsetAsync(red, 0, 10 * sizeof(double), h->stream));
+    SnFieldArgsHost a = field_args(h, r, nullptr, nullptr, h->d_red, 10);
+    sn_status s = launch_field(h, r, prec == SN_ENERGY_FP64, a);
+    if (s) return s;
+    SN_CK(h, sn_launch_recompute_finish(red, h->d_state, h->d_reps, r, h->params.cage_strain, h->d_drift, record,
+                                        h->stream));
+    h->launches++;
+    return SN_OK;
+}
+
+sn_status capture_graph(sn_handle *h)
+{
+    // configure function attributes outside the capture
+    for (int v = 0; v < 2; v++) SN_CK(h, k_sweep[h->rc](v == 1, h->mixed, SnPhaseArgs{}, 0, 0, h->stream));
+    cudaGraph_t g;
+    SN_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    uint64_t nodes = 0;
+    cudaError_t e = cudaSuccess;
+    for (int p = 0; p < 8 && e == cudaSuccess; p++)
+        for (int v = 0; v < 2 && e == cudaSuccess; v++) {
+            const int k = p * 2 + v;
+            if (!h->work_cnt[k]) continue;
+            SnPhaseArgs a;
+            a.work = h->d_work + h->work_off[k];
+            a.n_work = h->work_cnt[k];
+            a.reps = h->d_reps;
+            a.geoms = h->d_geoms;
+            a.acc = h->d_acc;
+            a.sweep = h->d_sweep;
+            a.cage = h->params.cage_strain;
+            a.K = h->params.K;
+            a.constrain = h->params.constrain_to_x;
+            a.dim = h->params.dim;
+            e = k_sweep[h->rc](v == 1, h->mixed, a, h->work_cnt[k], h->work_smem[k], h->stream);
+            nodes++;
+        }
+    if (e == cudaSuccess) {
+        e = sn_launch_sweep_end(h->d_acc, h->d_state, h->d_hist, h->d_reps, h->nrep, h->d_sweep, h->d_ex, h->d_order,
+                                h->stream);
+        nodes++;
+    }
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess) return fail(h, SN_ERR_CUDA, "sweep capture: %s", cudaGetErrorString(e));
+    if (e2 != cudaSuccess) return fail(h, SN_ERR_CUDA, "sweep capture end: %s", cudaGetErrorString(e2));
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(h, SN_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    h->graph_nodes = nodes;
+    return SN_OK;
+}
+
+void destroy_all(sn_handle *h)
+{
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (float *p : h->lattice_mem) cudaFree(p);
+    void *ptrs[] = {h->d_reps, h->d_geoms, h->d_acc, h->d_state, h->d_sweep, h->d_hist, h->d_red, h->d_drift,
+                    h->d_ex,   h->d_order, h->d_flags, h->d_work, h->d_stage, h->d_site, h->d_grad, h->d_trace};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char *sn_gpu_status_string(sn_status s)
+{
+    switch (s) {
+    case SN_OK: return "ok";
+    case SN_ERR_ARG: return "invalid argument";
+    case SN_ERR_CONFIG: return "invalid configuration";
+    case SN_ERR_SCHEDULE: return "no conflict-free schedule for this lattice";
+    case SN_ERR_CUDA: return "CUDA error";
+    case SN_ERR_NOMEM: return "out of memory";
+    case SN_ERR_TIMEOUT: return "device wait timed out";
+    case SN_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+const char *sn_gpu_last_error(const sn_handle *h)
+{
+    if (h && !h->err.empty()) return h->err.c_str();
+    return g_last_error.c_str();
+}
+
+int sn_neighbour_count(int cutoff, int Z)
+{
+    if (cutoff < 0) return 0;
+    int n = 0;
+    const int zc = Z == 1 ? 0 : cutoff;
+    for (int x = -cutoff; x <= cutoff; x++)
+        for (int y = -cutoff; y <= cutoff; y++)
+            for (int z = -zc; z <= zc; z++)
+                if ((x || y || z) && x * x + y * y + z * z <= cutoff * cutoff) n++;
+    return n;
+}
+
+sn_status sn_plan_schedule(int X, int Y, int Z, int cutoff, int mixed_lengths, sn_schedule_info *out)
+{
+    if (!out || X < 1 || Y < 1 || Z < 1) return fail(nullptr, SN_ERR_ARG, "bad lattice size or null output");
+    SnTile t;
+    std::string why;
+    if (cutoff < 1 || cutoff > SN_MAX_CUTOFF)
+        return fail(nullptr, SN_ERR_UNSUPPORTED, "cutoff %d outside 1..%d", cutoff, SN_MAX_CUTOFF);
+    if (!plan_tile(X, Y, Z, cutoff, mixed_lengths != 0, t, why)) return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
+    fill_info(t, cutoff, out);
+    return SN_OK;
+}
+
+int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *sc)
+{
+    if (!sc || X < 1 || Y < 1 || Z < 1 || cutoff < 1) return 0;
+    const bool two_d = Z == 1;
+    if (sc->bx * sc->nbx != X || sc->by * sc->nby != Y || sc->bz * sc->nbz != Z) return 0;
+    if (sc->nbx % sc->mx || sc->nby % sc->my || sc->nbz % sc->mz) return 0;
+    auto key = [&](int x, int y, int z) {
+        const int bx = x / sc->bx, by = y / sc->by, bz = z / sc->bz;
+        const int lx = x % sc->bx, ly = y % sc->by, lz = z % sc->bz;
+        long long k = ((bx % sc->mx) * sc->my + (by % sc->my)) * (long long)sc->mz + (bz % sc->mz);
+        k = ((k * sc->s + lx % sc->s) * sc->s + ly % sc->s) * sc->s + (two_d ? 0 : lz % sc->s);
+        return k;
+    };
+    const int zc = two_d ? 0 : cutoff;
+    for (int x = 0; x < X; x++)
+        for (int y = 0; y < Y; y++)
+            for (int z = 0; z < Z; z++) {
+                const long long k0 = key(x, y, z);
+                for (int dx = -cutoff; dx <= cutoff; dx++)
+                    for (int dy = -cutoff; dy <= cutoff; dy++)
+                        for (int dz = -zc; dz <= zc; dz++) {
+                            if (!(dx || dy || dz) || dx * dx + dy * dy + dz * dz > cutoff * cutoff) continue;
+                            const int x2 = ((x + dx) % X + X) % X, y2 = ((y + dy) % Y + Y) % Y,
+                                      z2 = ((z + dz) % Z + Z) % Z;
+                            if (x2 == x && y2 == y && z2 == z) return 0;  // a site that sees its own image
+                            if (key(x2, y2, z2) == k0) return 0;
+                        }
+            }
+    return 1;
+}
+
+sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_desc *replicas, sn_handle **out)
+{
+    if (!params || !replicas || !out || n_replicas < 1) return fail(nullptr, SN_ERR_ARG, "null argument or no replicas");
+    *out = nullptr;
+    const sn_params &P = *params;
+    if (P.cutoff < 1 || P.cutoff > SN_MAX_CUTOFF)
+        return fail(nullptr, SN_ERR_UNSUPPORTED, "DipoleCutOff=%d: this build has tiled kernels for 1..%d", P.cutoff,
+                    SN_MAX_CUTOFF);
+    if (P.dim != 2 && P.dim != 3) return fail(nullptr, SN_ERR_CONFIG, "dim must be 2 or 3");
+    if (P.n_species < 1 || P.n_species > SN_MAX_SPECIES)
+        return fail(nullptr, SN_ERR_CONFIG, "n_species must be 1..%d", SN_MAX_SPECIES);
+    float L = 0.0f;
+    bool mixed = false;
+    for (int i = 0; i < P.n_species; i++) {
+        const float d = P.dipoles[i];
+        if (!(d >= 0.0f) || std::isinf(d)) return fail(nullptr, SN_ERR_CONFIG, "Dipoles[%d] must be finite and >= 0", i);
+        if (!(P.prevalence[i] >= 0.0f)) return fail(nullptr, SN_ERR_CONFIG, "Prevalence[%d] must be >= 0", i);
+        if (d > 0.0f) {
+            if (L == 0.0f) L = d;
+            else if (d != L) mixed = true;
+        }
+    }
+    for (int r = 0; r < n_replicas; r++) {
+        const sn_replica_desc &d = replicas[r];
+        if (d.X < 1 || d.Y < 1 || d.Z < 1) return fail(nullptr, SN_ERR_ARG, "replica %d: bad size", r);
+        if ((long long)d.X * d.Y * d.Z > 0x7fffffffLL)
+            return fail(nullptr, SN_ERR_UNSUPPORTED, "replica %d: more than 2^31-1 sites", r);
+        if (!(d.T > 0.0f)) return fail(nullptr, SN_ERR_ARG, "replica %d: temperature must be > 0", r);
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+        return fail(nullptr, SN_ERR_CUDA, "no CUDA device available");
+
+    sn_handle *h = new sn_handle();
+    h->params = P;
+    h->nrep = n_replicas;
+    h->mixed = mixed;
+    h->length = L;
+    h->dipole_ref = L;
+    h->rc = P.cutoff;
+    h->desc.assign(replicas, replicas + n_replicas);
+    h->tiles.resize(n_replicas);
+    h->reps.resize(n_replicas);
+    h->work_off.assign(16, 0);
+    h->work_cnt.assign(16, 0);
+    h->work_smem.assign(16, 0);
+    h->fwork_off.assign(n_replicas, 0);
+    h->fwork_cnt.assign(n_replicas, 0);
+
+    auto bail = [&](sn_status s) {
+        std::string msg = h->err;
+        destroy_all(h);
+        g_last_error = msg;
+        return s;
+    };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(h, SN_ERR_CUDA, "cudaStreamCreate failed"));
+
+    for (int r = 0; r < n_replicas; r++) {
+        std::string why;
+        const sn_replica_desc &d = replicas[r];
+        if (!plan_tile(d.X, d.Y, d.Z, P.cutoff, mixed, h->tiles[r], why))
+            return bail(fail(h, SN_ERR_SCHEDULE, "replica %d (%dx%dx%d): %s", r, d.X, d.Y, d.Z, why.c_str()));
+        const long long N = (long long)d.X * d.Y * d.Z;
+        float *mem = nullptr;
+        if (cudaMalloc(&mem, 4 * N * sizeof(float)) != cudaSuccess)
+            return bail(fail(h, SN_ERR_NOMEM, "replica %d: cannot allocate %lld sites", r, N));
+        h->lattice_mem.push_back(mem);
+        if (cudaMemsetAsync(mem, 0, 4 * N * sizeof(float), h->stream) != cudaSuccess)
+            return bail(fail(h, SN_ERR_CUDA, "cudaMemset failed"));
+        SnReplicaDev &R = h->reps[r];
+        memset(&R, 0, sizeof(R));
+        R.px = mem;
+        R.py = mem + N;
+        R.pz = mem + 2 * N;
+        R.len = mem + 3 * N;
+        R.X = d.X;
+        R.Y = d.Y;
+        R.Z = d.Z;
+        R.geom = r;
+        R.n_sites = N;
+        R.T = d.T;
+        R.beta = (float)(300.0 / (double)d.T);
+        for (int k = 0; k < 3; k++) R.E[k] = d.has_efield ? d.efield[k] : P.efield[k];
+        R.length = L;
+        const uint64_t seed = d.seed ? d.seed : P.seed + (uint64_t)r;
+        R.seed_lo = (uint32_t)seed;
+        R.seed_hi = (uint32_t)(seed >> 32);
+    }
+
+    // work lists: per block colour and kernel variant (3D, 2D), then all blocks per replica
+    std::vector<SnWork> work;
+    for (int p = 0; p < 8; p++)
+        for (int v = 0; v < 2; v++) {
+            const int k = p * 2 + v;
+            h->work_off[k] = (int)work.size();
+            const int cb[3] = {(p >> 2) & 1, (p >> 1) & 1, p & 1};
+            for (int r = 0; r < n_replicas; r++) {
+                const bool two_d = replicas[r].Z == 1;
+                if ((v == 1) != two_d) continue;
+                const SnTile &t = h->tiles[r];
+                for (int bx = 0; bx < t.nb[0]; bx++)
+                    for (int by = 0; by < t.nb[1]; by++)
+                        for (int bz = 0; bz < t.nb[2]; bz++) {
+                            if (bx % t.m[0] != cb[0] || by % t.m[1] != cb[1] || bz % t.m[2] != cb[2]) continue;
+                            work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
+                            h->work_smem[k] = std::max(h->work_smem[k], t.smem_bytes);
+                        }
+            }
+            h->work_cnt[k] = (int)work.size() - h->work_off[k];
+        }
+    for (int r = 0; r < n_replicas; r++) {
+        const SnTile &t = h->tiles[r];
+        h->fwork_off[r] = (int)work.size();
+        for (int bx = 0; bx < t.nb[0]; bx++)
+            for (int by = 0; by < t.nb[1]; by++)
+                for (int bz = 0; bz < t.nb[2]; bz++) work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
+        h->fwork_cnt[r] = (int)work.size() - h->fwork_off[r];
+    }
+
+    // temperature ladder for exchange: replicas sorted by T
+    std::vector<int> order(n_replicas);
+    for (int r = 0; r < n_replicas; r++) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return replicas[a].T < replicas[b].T; });
+
+    const size_t nr = (size_t)n_replicas;
+#define ALLOC(ptr, bytes)                                                                         \
+    if (cudaMalloc((void **)&(ptr), (bytes)) != cudaSuccess ||                                    \
+        cudaMemsetAsync((void *)(ptr), 0, (bytes), h->stream) != cudaSuccess)                     \
+        return bail(fail(h, SN_ERR_NOMEM, "device allocation of %zu bytes failed", (size_t)(bytes)));
+    ALLOC(h->d_reps, nr * sizeof(SnReplicaDev));
+    ALLOC(h->d_geoms, nr * sizeof(SnTile));
+    ALLOC(h->d_acc, nr * sizeof(SnAccum));
+    ALLOC(h->d_state, nr * sizeof(SnState));
+    ALLOC(h->d_sweep, sizeof(uint32_t));
+    ALLOC(h->d_hist, nr * SN_HIST_CAP * 2 * sizeof(double));
+    ALLOC(h->d_red, nr * 10 * sizeof(double));
+    ALLOC(h->d_drift, nr * sizeof(double));
+    ALLOC(h->d_ex, sizeof(SnExchange));
+    ALLOC(h->d_order, nr * sizeof(int));
+    ALLOC(h->d_flags, 4 * sizeof(int));
+    ALLOC(h->d_work, std::max<size_t>(work.size(), 1) * sizeof(SnWork));
+#undef ALLOC
+    SnExchange ex;
+    memset(&ex, 0, sizeof(ex));
+    ex.seed_lo = (uint32_t)(P.seed ^ 0x5A5A5A5Aull);
+    ex.seed_hi = (uint32_t)((P.seed >> 32) ^ 0xA5A5A5A5ull);
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_reps, h->reps.data(), nr * sizeof(SnReplicaDev), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_geoms, h->tiles.data(), nr * sizeof(SnTile), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_work, work.data(), work.size() * sizeof(SnWork), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_order, order.data(), nr * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_ex, &ex, sizeof(ex), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return bail(fail(h, SN_ERR_CUDA, "init upload: %s", cudaGetErrorString(e)));
+    sn_status s = capture_graph(h);
+    if (s) return bail(s);
+    *out = h;
+    return SN_OK;
+}
+
+sn_status sn_gpu_destroy(sn_handle *h)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    destroy_all(h);
+    return SN_OK;
+}
+
+sn_status sn_gpu_init_lattice(sn_handle *h, int replica, int pattern, uint64_t seed)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (pattern != SN_LATTICE_RANDOM && pattern != SN_LATTICE_FERROELECTRIC)
+        return fail(h, SN_ERR_ARG, "unknown lattice pattern %d", pattern);
+    const SnReplicaDev &R = h->reps[replica];
+    SnInitArgs a;
+    memset(&a, 0, sizeof(a));
+    a.px = R.px;
+    a.py = R.py;
+    a.pz = R.pz;
+    a.len = R.len;
+    a.n = R.n_sites;
+    a.pattern = pattern;
+    a.dim = h->params.dim;
+    a.n_species = h->params.n_species;
+    for (int i = 0; i < h->params.n_species; i++) {
+        a.dipoles[i] = h->params.dipoles[i];
+        a.prevalence[i] = h->params.prevalence[i];
+    }
+    if (!seed) seed = ((uint64_t)R.seed_hi << 32) | R.seed_lo;
+    a.seed_lo = (uint32_t)seed;
+    a.seed_hi = (uint32_t)(seed >> 32);
+    SN_CK(h, sn_launch_init_lattice(a, h->stream));
+    h->launches++;
+    s = recompute_one(h, replica, SN_ENERGY_FP32, 0);
+    if (s) return s;
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_upload_lattice(sn_handle *h, int replica, const float *xyz, const float *len)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (!xyz) return fail(h, SN_ERR_ARG, "null xyz buffer");
+    const SnReplicaDev &R = h->reps[replica];
+    const size_t N = (size_t)R.n_sites;
+    s = ensure(h, (void **)&h->d_stage, &h->stage_floats, 4 * N, sizeof(float));
+    if (s) return s;
+    SN_CK(h, cudaMemcpyAsync(h->d_stage, xyz, 3 * N * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    if (len) SN_CK(h, cudaMemcpyAsync(h->d_stage + 3 * N, len, N * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    SN_CK(h, cudaMemsetAsync(h->d_flags, 0, 4 * sizeof(int), h->stream));
+    SN_CK(h, sn_launch_upload_convert(h->d_stage, len ? h->d_stage + 3 * N : nullptr, R.px, R.py, R.pz, R.len,
+                                      (long long)N, h->length, h->mixed ? 1 : 0, h->params.dipoles[0], h->d_flags,
+                                      h->stream));
+    h->launches++;
+    int flags[4] = {0, 0, 0, 0};
+    SN_CK(h, cudaMemcpyAsync(flags, h->d_flags, sizeof(flags), cudaMemcpyDeviceToHost, h->stream));
+    s = recompute_one(h, replica, SN_ENERGY_FP32, 0);
+    if (s) return s;
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if (flags[2]) return fail(h, SN_ERR_ARG, "negative or non-finite dipole length in upload");
+    if (flags[0])
+        return fail(h, SN_ERR_ARG, "upload has a dipole length other than %g, but the handle was created for a single "
+                                   "species length (list every species in sn_params.dipoles)", (double)h->length);
+    if (flags[1]) return fail(h, SN_ERR_ARG, "an occupied site (length > 0) holds the zero vector");
+    return SN_OK;
+}
+
+sn_status sn_gpu_download_lattice(sn_handle *h, int replica, float *xyz, float *len)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (!xyz && !len) return fail(h, SN_ERR_ARG, "null output buffers");
+    const SnReplicaDev &R = h->reps[replica];
+    const size_t N = (size_t)R.n_sites;
+    s = ensure(h, (void **)&h->d_stage, &h->stage_floats, 4 * N, sizeof(float));
+    if (s) return s;
+    SN_CK(h, sn_launch_download_convert(R.px, R.py, R.pz, R.len, h->d_stage, h->d_stage + 3 * N, (long long)N,
+                                        h->stream));
+    h->launches++;
+    if (xyz) SN_CK(h, cudaMemcpyAsync(xyz, h->d_stage, 3 * N * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    if (len) SN_CK(h, cudaMemcpyAsync(len, h->d_stage + 3 * N, N * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *reject)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    if (n_sweeps < 0) return fail(h, SN_ERR_ARG, "negative sweep count");
+    std::vector<SnState> before;
+    if (accept || reject) {
+        before.resize(h->nrep);
+        SN_CK(h, cudaMemcpyAsync(before.data(), h->d_state, h->nrep * sizeof(SnState), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    }
+    for (int i = 0; i < n_sweeps; i++) {
+        SN_CK(h, cudaGraphLaunch(h->graph, h->stream));
+        h->launches += h->graph_nodes;
+        h->sweeps++;
+        if (h->recompute_every > 0 && h->sweeps % (uint64_t)h->recompute_every == 0) {
+            for (int r = 0; r < h->nrep; r++) {
+                sn_status s = recompute_one(h, r, h->recompute_prec, 1);
+                if (s) return s;
+            }
+            h->n_checks++;
+        }
+    }
+    if (accept || reject) {
+        std::vector<SnState> after(h->nrep);
+        SN_CK(h, cudaMemcpyAsync(after.data(), h->d_state, h->nrep * sizeof(SnState), cudaMemcpyDeviceToHost, h->stream));
+        SN_CK(h, cudaStreamSynchronize(h->stream));
+        uint64_t a = 0, t = 0;
+        for (int r = 0; r < h->nrep; r++) {
+            a += after[r].acc_total - before[r].acc_total;
+            t += after[r].att_total - before[r].att_total;
+        }
+        if (accept) *accept = a;
+        if (reject) *reject = t - a;
+    }
+    SN_CK(h, cudaGetLastError());
+    return SN_OK;
+}
+
+sn_status sn_gpu_sweep_count(const sn_handle *h, uint64_t *sweeps)
+{
+    if (!h || !sweeps) return fail(nullptr, SN_ERR_ARG, "null argument");
+    *sweeps = h->sweeps;
+    return SN_OK;
+}
+
+sn_status sn_gpu_energy(sn_handle *h, int replica, int precision, double *E_total, double *site_E)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    const size_t N = (size_t)h->reps[replica].n_sites;
+    if (site_E) {
+        s = ensure(h, (void **)&h->d_site, &h->site_n, N, sizeof(double));
+        if (s) return s;
+    }
+    double *red = h->d_red + 10 * replica;
+    SN_CK(h, cudaMemsetAsync(red, 0, 10 * sizeof(double), h->stream));
+    SnFieldArgsHost a = field_args(h, replica, site_E ? h->d_site : nullptr, nullptr, h->d_red, 10);
+    s = launch_field(h, replica, precision == SN_ENERGY_FP64, a);
+    if (s) return s;
+    double hr[10];
+    SN_CK(h, cudaMemcpyAsync(hr, red, sizeof(hr), cudaMemcpyDeviceToHost, h->stream));
+    if (site_E) SN_CK(h, cudaMemcpyAsync(site_E, h->d_site, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if (E_total) *E_total = hr[0] - 0.5 * (double)h->params.cage_strain * hr[1] + hr[2] + hr[3];
+    return SN_OK;
+}
+
+sn_status sn_gpu_observables(sn_handle *h, double *E_per_site, double *P_abs, double *P_vec)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    std::vector<SnState> st(h->nrep);
+    SN_CK(h, cudaMemcpyAsync(st.data(), h->d_state, h->nrep * sizeof(SnState), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    for (int r = 0; r < h->nrep; r++) {
+        const double N = (double)h->reps[r].n_sites;
+        if (E_per_site) E_per_site[r] = st[r].E / N;
+        if (P_abs) P_abs[r] = std::sqrt(st[r].P[0] * st[r].P[0] + st[r].P[1] * st[r].P[1] + st[r].P[2] * st[r].P[2]) / N;
+        if (P_vec)
+            for (int k = 0; k < 3; k++) P_vec[3 * r + k] = st[r].P[k];
+    }
+    return SN_OK;
+}
+
+sn_status sn_gpu_history(sn_handle *h, int replica, int max, double *E_per_site, double *P_abs, int *n_out)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (max < 0 || !n_out) return fail(h, SN_ERR_ARG, "bad history buffer");
+    SnState st;
+    SN_CK(h, cudaMemcpyAsync(&st, h->d_state + replica, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    std::vector<double> ring((size_t)SN_HIST_CAP * 2);
+    SN_CK(h, cudaMemcpyAsync(ring.data(), h->d_hist + (size_t)replica * SN_HIST_CAP * 2, ring.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    const int have = std::min(st.hist_head, SN_HIST_CAP);
+    const int n = std::min(have, max);
+    const int first = st.hist_head - n;
+    for (int i = 0; i < n; i++) {
+        const int k = (first + i) % SN_HIST_CAP;
+        if (E_per_site) E_per_site[i] = ring[2 * k];
+        if (P_abs) P_abs[i] = ring[2 * k + 1];
+    }
+    *n_out = n;
+    const int zero = 0;
+    SN_CK(h, cudaMemcpyAsync(&h->d_state[replica].hist_head, &zero, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_recompute(sn_handle *h, int precision, double *max_rel_drift)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    SN_CK(h, cudaMemsetAsync(h->d_drift, 0, h->nrep * sizeof(double), h->stream));
+    for (int r = 0; r < h->nrep; r++) {
+        sn_status s = recompute_one(h, r, precision, 1);
+        if (s) return s;
+    }
+    std::vector<double> d(h->nrep);
+    SN_CK(h, cudaMemcpyAsync(d.data(), h->d_drift, h->nrep * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if (max_rel_drift) *max_rel_drift = d.empty() ? 0.0 : *std::max_element(d.begin(), d.end());
+    SN_CK(h, cudaMemsetAsync(h->d_drift, 0, h->nrep * sizeof(double), h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_set_recompute(sn_handle *h, int every, int precision)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    if (every < 0) return fail(h, SN_ERR_ARG, "negative interval");
+    h->recompute_every = every;
+    h->recompute_prec = precision;
+    return SN_OK;
+}
+
+sn_status sn_gpu_drift(const sn_handle *h, double *max_rel_drift, int *n_checks)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    std::vector<double> d(h->nrep);
+    cudaError_t e = cudaMemcpyAsync(d.data(), h->d_drift, h->nrep * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail(const_cast<sn_handle *>(h), SN_ERR_CUDA, "drift read: %s", cudaGetErrorString(e));
+    if (max_rel_drift) *max_rel_drift = *std::max_element(d.begin(), d.end());
+    if (n_checks) *n_checks = h->n_checks;
+    return SN_OK;
+}
+
+sn_status sn_gpu_set_field(sn_handle *h, int replica, const float efield[3])
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (!efield) return fail(h, SN_ERR_ARG, "null field");
+    for (int k = 0; k < 3; k++) h->reps[replica].E[k] = efield[k];
+    SN_CK(h, cudaMemcpyAsync(&h->d_reps[replica].E, h->reps[replica].E, 3 * sizeof(float), cudaMemcpyHostToDevice,
+                             h->stream));
+    // the field term changes the running energy: restart it from a recompute
+    s = recompute_one(h, replica, SN_ENERGY_FP32, 0);
+    if (s) return s;
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_set_temperature(sn_handle *h, int replica, float T)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (!(T > 0.0f)) return fail(h, SN_ERR_ARG, "temperature must be > 0");
+    SnReplicaDev cur;
+    SN_CK(h, cudaMemcpyAsync(&cur, h->d_reps + replica, sizeof(cur), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    cur.T = T;
+    cur.beta = (float)(300.0 / (double)T);
+    h->reps[replica].T = cur.T;
+    h->reps[replica].beta = cur.beta;
+    SN_CK(h, cudaMemcpyAsync(h->d_reps + replica, &cur, sizeof(cur), cudaMemcpyHostToDevice, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_get_temperature(const sn_handle *h, int replica, float *T)
+{
+    if (!h || !T) return fail(nullptr, SN_ERR_ARG, "null argument");
+    if (replica < 0 || replica >= h->nrep) return fail(const_cast<sn_handle *>(h), SN_ERR_ARG, "replica out of range");
+    SnReplicaDev cur;
+    cudaError_t e = cudaMemcpyAsync(&cur, h->d_reps + replica, sizeof(cur), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail(const_cast<sn_handle *>(h), SN_ERR_CUDA, "%s", cudaGetErrorString(e));
+    *T = cur.T;
+    return SN_OK;
+}
+
+sn_status sn_gpu_set_exchange(sn_handle *h, int every)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    if (every < 0) return fail(h, SN_ERR_ARG, "negative interval");
+    h->exchange_every = every;
+    SN_CK(h, cudaMemcpyAsync(&h->d_ex->every, &h->exchange_every, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_exchange_stats(sn_handle *h, uint64_t *attempted, uint64_t *accepted)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    SnExchange ex;
+    SN_CK(h, cudaMemcpyAsync(&ex, h->d_ex, sizeof(ex), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if (attempted) *attempted = ex.attempted;
+    if (accepted) *accepted = ex.accepted;
+    return SN_OK;
+}
+
+sn_status sn_gpu_adjoint(sn_handle *h, int replica, float *dE_dp, double *dE_dparams, double *E_total)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    const size_t N = (size_t)h->reps[replica].n_sites;
+    if (dE_dp) {
+        s = ensure(h, (void **)&h->d_grad, &h->grad_n, 3 * N, sizeof(float));
+        if (s) return s;
+    }
+    double *red = h->d_red + 10 * replica;
+    SN_CK(h, cudaMemsetAsync(red, 0, 10 * sizeof(double), h->stream));
+    SnFieldArgsHost a = field_args(h, replica, nullptr, dE_dp ? h->d_grad : nullptr, h->d_red, 10);
+    s = launch_field(h, replica, false, a);
+    if (s) return s;
+    double hr[10];
+    SN_CK(h, cudaMemcpyAsync(hr, red, sizeof(hr), cudaMemcpyDeviceToHost, h->stream));
+    if (dE_dp) SN_CK(h, cudaMemcpyAsync(dE_dp, h->d_grad, 3 * N * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if (dE_dparams) {
+        dE_dparams[0] = h->dipole_ref != 0.0f ? 2.0 * hr[0] / (double)h->dipole_ref : 0.0;
+        dE_dparams[1] = -0.5 * hr[1];
+        dE_dparams[2] = hr[7];
+        dE_dparams[3] = hr[8];
+        dE_dparams[4] = hr[9];
+    }
+    if (E_total) *E_total = hr[0] - 0.5 * (double)h->params.cage_strain * hr[1] + hr[2] + hr[3];
+    return SN_OK;
+}
+
+sn_status sn_gpu_quench(sn_handle *h, int replica, int n_steps, float step, double *E_trace)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (n_steps < 0 || !(step > 0.0f)) return fail(h, SN_ERR_ARG, "need n_steps >= 0 and step > 0");
+    const SnReplicaDev &R = h->reps[replica];
+    const size_t N = (size_t)R.n_sites;
+    s = ensure(h, (void **)&h->d_grad, &h->grad_n, 3 * N, sizeof(float));
+    if (s) return s;
+    s = ensure(h, (void **)&h->d_trace, &h->trace_n, 10 * (size_t)(n_steps + 1), sizeof(double));
+    if (s) return s;
+    SN_CK(h, cudaMemsetAsync(h->d_trace, 0, 10 * (size_t)(n_steps + 1) * sizeof(double), h->stream));
+    for (int k = 0; k <= n_steps; k++) {
+        SnFieldArgsHost a = field_args(h, replica, nullptr, k < n_steps ? h->d_grad : nullptr, h->d_trace + 10 * k, 0);
+        s = launch_field(h, replica, false, a);
+        if (s) return s;
+        if (k < n_steps) {
+            SN_CK(h, sn_launch_quench_step(R.px, R.py, R.pz, R.len, h->d_grad, (long long)N, step, h->stream));
+            h->launches++;
+        }
+    }
+    std::vector<double> tr(10 * (size_t)(n_steps + 1));
+    SN_CK(h, cudaMemcpyAsync(tr.data(), h->d_trace, tr.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    s = recompute_one(h, replica, SN_ENERGY_FP32, 0);
+    if (s) return s;
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if (E_trace)
+        for (int k = 0; k <= n_steps; k++) {
+            const double *r = &tr[10 * (size_t)k];
+            E_trace[k] = r[0] - 0.5 * (double)h->params.cage_strain * r[1] + r[2] + r[3];
+        }
+    return SN_OK;
+}
+
+sn_status sn_gpu_schedule(const sn_handle *h, int replica, sn_schedule_info *out)
+{
+    if (!h || !out) return fail(nullptr, SN_ERR_ARG, "null argument");
+    if (replica < 0 || replica >= h->nrep) return fail(const_cast<sn_handle *>(h), SN_ERR_ARG, "replica out of range");
+    fill_info(h->tiles[replica], h->rc, out);
+    return SN_OK;
+}
+
+sn_status sn_gpu_launch_count(const sn_handle *h, uint64_t *launches)
+{
+    if (!h || !launches) return fail(nullptr, SN_ERR_ARG, "null argument");
+    *launches = h->launches;
+    return SN_OK;
+}
+
+void *sn_gpu_stream(const sn_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+sn_status sn_gpu_philox(const uint32_t *ctr, const uint32_t *key, uint32_t *out, int n)
+{
+    if (!ctr || !key || !out || n < 0) return fail(nullptr, SN_ERR_ARG, "null buffer or negative count");
+    if (n == 0) return SN_OK;
+    uint32_t *d = nullptr;
+    if (cudaMalloc(&d, (size_t)n * 10 * sizeof(uint32_t)) != cudaSuccess)
+        return fail(nullptr, SN_ERR_NOMEM, "cudaMalloc failed");
+    cudaError_t e = cudaMemcpy(d, ctr, (size_t)n * 4 * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + 4 * (size_t)n, key, (size_t)n * 2 * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = sn_launch_philox_batch(d, d + 4 * (size_t)n, d + 6 * (size_t)n, n, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 6 * (size_t)n, (size_t)n * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(nullptr, SN_ERR_CUDA, "philox batch: %s", cudaGetErrorString(e));
+    return SN_OK;
+}
+
+sn_status sn_gpu_proposals(const sn_handle *h, int replica, const uint32_t *sites, int n, uint32_t sweep, float *out4)
+{
+    if (!h || !sites || !out4 || n < 0) return fail(nullptr, SN_ERR_ARG, "null argument");
+    if (replica < 0 || replica >= h->nrep) return fail(const_cast<sn_handle *>(h), SN_ERR_ARG, "replica out of range");
+    if (n == 0) return SN_OK;
+    const SnReplicaDev &R = h->reps[replica];
+    void *d = nullptr;
+    if (cudaMalloc(&d, (size_t)n * 5 * sizeof(uint32_t)) != cudaSuccess)
+        return fail(const_cast<sn_handle *>(h), SN_ERR_NOMEM, "cudaMalloc failed");
+    uint32_t *ds = (uint32_t *)d;
+    float *dout = (float *)(ds + n);
+    cudaError_t e = cudaMemcpyAsync(ds, sites, (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = sn_launch_proposal_batch(ds, sweep, R.seed_lo, R.seed_hi, h->params.dim, h->params.constrain_to_x, dout, n,
+                                     h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out4, dout, (size_t)n * 4 * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(const_cast<sn_handle *>(h), SN_ERR_CUDA, "proposal batch: %s", cudaGetErrorString(e));
+    return SN_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// sn_internal.h -- structures shared by the host side and the kernels.
+//
+// Device data layout (one replica = one lattice):
+//   px, py, pz, len : SoA float arrays of N = X*Y*Z sites, index (x*Y+y)*Z+z
+//                     (z fastest, the reference's lattice[x][y][z] order).
+//   Vacancies (len == 0) hold the zero vector, so in uniform-length mode the
+//   sweep kernel reads only px/py/pz and a zero vector marks a vacancy.
+#pragma once
+
+#include <cstdint>
+
+#define SN_THREADS 256           // threads per sweep block
+#define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
+#define SN_HIST_CAP 4096         // per-replica per-sweep observable log
+
+// Geometry of one replica's tiles: block dims, tile dims (block + halo),
+// and the per-axis permutation that stores each axis class-major
+// (coordinates u with the same u mod s contiguous).  Slot of tile
+// coordinate (ux,uy,uz) = pi_x(ux)*Sx + pi_y(uy)*Sy + pi_z(uz), with
+// pi_a(u) = start[a][u mod s] + u / s.
+struct SnTile {
+    int B[3];        // block dims
+    int T[3];        // tile dims = B + 2*halo (z: 1 in 2D)
+    int H[3];        // halo per axis
+    int nb[3];       // blocks per axis
+    int m[3];        // block colours per axis
+    int Sy, Sx;      // padded slot strides (z stride is 1)
+    int slots;       // Sx * T[0]
+    int maxt;        // max targets of one site colour inside a block
+    int start[3][SN_MAX_S];
+    int smem_bytes;  // dynamic shared memory for the sweep kernel
+};
+
+struct SnReplicaDev {
+    float *px, *py, *pz, *len;
+    int X, Y, Z;
+    int geom;          // index into the SnTile table
+    long long n_sites;
+    float beta;        // 300 / T
+    float T;
+    float E[3];        // applied field
+    float length;      // uniform dipole length (uniform mode)
+    uint32_t seed_lo, seed_hi;
+};
+
+// Per-replica sweep accumulators (zeroed at the end of every sweep).
+struct SnAccum {
+    double dE;
+    double dP[3];
+    unsigned long long acc;
+    unsigned long long att;
+};
+
+// Per-replica running state.
+struct SnState {
+    double E;           // running FP64 total energy
+    double P[3];        // running FP64 sum_i len_i p_i
+    unsigned long long acc_total, att_total;
+    int hist_head;      // entries written since the last read (ring)
+    int pad;
+};
+
+struct SnWork {
+    int rep;
+    int x0, y0, z0;     // block origin
+};
+
+struct SnPhaseArgs {
+    const SnWork *work;
+    int n_work;
+    const SnReplicaDev *reps;
+    const SnTile *geoms;
+    SnAccum *acc;
+    const uint32_t *sweep;   // device sweep counter
+    float cage;
+    float K;
+    int constrain;
+    int dim;
+};
+
+// Neighbour offset table for the per-site kernels (energy, adjoint, quench).
+struct SnNeighbour {
+    int dx, dy, dz, unit;
+    double T[6];        // xx yy zz xy xz yz of (I - 3 n n^T) / d^3
+    float Tf[6];
+    float pad[2];
+};

@@ -1,0 +1,272 @@
+// sn_kernels.cu -- the small kernels around the sweep: lattice
+// initialisation, host-layout conversion, the end-of-sweep fold with replica
+// exchange, recompute bookkeeping and the quench step.
+#include <cmath>
+
+#include "../../include/sn_gpu.h"
+#include "sn_device.cuh"
+#include "sn_launch.h"
+
+namespace {
+
+// initialise_lattice_random / _ferroelectric + solid_solution
+// (src/starrynight-lattice.c:25-47, :139-171), drawn from Philox with
+// counter (site, 0, k, SN_STREAM_INIT).  Draw 0 word 0 picks the species by
+// walking the Prevalence list as solid_solution does; words 1,2 and later
+// draws feed the same Marsaglia tries as the sweep proposal.  Vacancies hold
+// the zero vector.
+__global__ void init_lattice_kernel(const SnInitArgs a)
+{
+    const uint2 key = make_uint2(a.seed_lo, a.seed_hi);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.n;
+         i += (long long)gridDim.x * blockDim.x) {
+        uint4 r = sn_philox(make_uint4((uint32_t)i, 0u, 0u, SN_STREAM_INIT), key);
+        float sample = sn_uniform24(r.x);
+        int s = 0;
+        while (s < a.n_species - 1 && sample > a.prevalence[s]) {
+            sample = __fsub_rn(sample, a.prevalence[s]);
+            s++;
+        }
+        const float L = a.dipoles[s];
+        float3 p = make_float3(1.0f, 0.0f, 0.0f);
+        if (a.pattern == SN_LATTICE_RANDOM) {
+            bool ok = sn_try_point(r.y, r.z, a.dim, p);
+            for (uint32_t k = 1; !ok && k < SN_PROPOSAL_MAX_DRAWS; k++) {
+                r = sn_philox(make_uint4((uint32_t)i, 0u, k, SN_STREAM_INIT), key);
+                ok = sn_try_point(r.x, r.y, a.dim, p) || sn_try_point(r.z, r.w, a.dim, p);
+            }
+            if (!ok) p = make_float3(0.0f, 0.0f, 1.0f);
+        }
+        if (L == 0.0f) p = make_float3(0.0f, 0.0f, 0.0f);
+        a.px[i] = p.x;
+        a.py[i] = p.y;
+        a.pz[i] = p.z;
+        a.len[i] = L;
+    }
+}
+
+// flags[0]: a length that differs from the uniform length (uniform mode)
+// flags[1]: an occupied site holding the zero vector
+// flags[2]: a negative or non-finite length
+__global__ void upload_convert_kernel(const float *__restrict__ sxyz, const float *__restrict__ slen, float *px,
+                                      float *py, float *pz, float *len, long long n, float uniform_len, int mixed,
+                                      float default_len, int *flags)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float x = sxyz[3 * i + 0], y = sxyz[3 * i + 1], z = sxyz[3 * i + 2];
+        const float L = slen ? slen[i] : default_len;
+        if (!(L >= 0.0f) || isinf(L)) atomicOr(&flags[2], 1);
+        if (L == 0.0f) {
+            x = y = z = 0.0f;
+        } else {
+            if (!mixed && L != uniform_len) atomicOr(&flags[0], 1);
+            if (x == 0.0f && y == 0.0f && z == 0.0f) atomicOr(&flags[1], 1);
+        }
+        px[i] = x;
+        py[i] = y;
+        pz[i] = z;
+        len[i] = L;
+    }
+}
+
+__global__ void download_convert_kernel(const float *__restrict__ px, const float *__restrict__ py,
+                                        const float *__restrict__ pz, const float *__restrict__ len, float *sxyz,
+                                        float *slen, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        sxyz[3 * i + 0] = px[i];
+        sxyz[3 * i + 1] = py[i];
+        sxyz[3 * i + 2] = pz[i];
+        if (slen) slen[i] = len[i];
+    }
+}
+
+// End of one sweep: fold the per-sweep accumulators into the running FP64
+// totals, log E/site and |P|/site, advance the sweep counter and, when due,
+// run one round of replica exchange between adjacent temperatures.
+__global__ void sweep_end_kernel(SnAccum *acc, SnState *state, double *hist, SnReplicaDev *reps, int nrep,
+                                 uint32_t *sweep, SnExchange *ex, int *order)
+{
+    for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
+        SnState &s = state[r];
+        SnAccum &A = acc[r];
+        s.E += A.dE;
+        s.P[0] += A.dP[0];
+        s.P[1] += A.dP[1];
+        s.P[2] += A.dP[2];
+        s.acc_total += A.acc;
+        s.att_total += A.att;
+        A.dE = 0.0;
+        A.dP[0] = A.dP[1] = A.dP[2] = 0.0;
+        A.acc = 0ull;
+        A.att = 0ull;
+        const double N = (double)reps[r].n_sites;
+        const double Pm = sqrt(s.P[0] * s.P[0] + s.P[1] * s.P[1] + s.P[2] * s.P[2]);
+        double *hr = hist + 2 * ((size_t)r * SN_HIST_CAP + (size_t)(s.hist_head % SN_HIST_CAP));
+        hr[0] = s.E / N;
+        hr[1] = Pm / N;
+        s.hist_head++;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t s = *sweep + 1u;
+        if (ex->every > 0 && nrep > 1 && (s % (uint32_t)ex->every) == 0u) {
+            const uint32_t round = s / (uint32_t)ex->every;
+            const uint2 key = make_uint2(ex->seed_lo, ex->seed_hi);
+            for (int k = (int)(round & 1u); k + 1 < nrep; k += 2) {
+                const int ra = order[k], rb = order[k + 1];
+                const double d = ((double)reps[ra].beta - (double)reps[rb].beta) * (state[ra].E - state[rb].E);
+                const uint4 q = sn_philox(make_uint4((uint32_t)k, round, 0u, SN_STREAM_EXCHANGE), key);
+                const double u = (double)sn_uniform24(q.x);
+                ex->attempted++;
+                if (d >= 0.0 || u < exp(d)) {
+                    const float tb = reps[ra].beta, tt = reps[ra].T;
+                    reps[ra].beta = reps[rb].beta;
+                    reps[ra].T = reps[rb].T;
+                    reps[rb].beta = tb;
+                    reps[rb].T = tt;
+                    order[k] = rb;
+                    order[k + 1] = ra;
+                    ex->accepted++;
+                }
+            }
+        }
+        *sweep = s;
+    }
+}
+
+// red (10 doubles, see SnFieldArgs) -> running E and P of one replica.
+__global__ void recompute_finish_kernel(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
+                                        float cage, double *drift_max, int record)
+{
+    const double E = red[0] - 0.5 * (double)cage * red[1] + red[2] + red[3];
+    SnState &s = state[rep];
+    if (record) {
+        const double d = fabs(s.E - E) / fmax(fabs(E), 1.0);
+        if (d > drift_max[rep]) drift_max[rep] = d;
+    }
+    s.E = E;
+    s.P[0] = red[4];
+    s.P[1] = red[5];
+    s.P[2] = red[6];
+    (void)reps;
+}
+
+// One projected-gradient step on the sphere at every occupied site:
+// p <- normalize(p - step (g - (g.p) p)).
+__global__ void quench_step_kernel(float *px, float *py, float *pz, const float *__restrict__ len,
+                                   const float *__restrict__ grad, long long n, float step)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        if (len[i] == 0.0f) continue;
+        const float x = px[i], y = py[i], z = pz[i];
+        const float gx = grad[3 * i], gy = grad[3 * i + 1], gz = grad[3 * i + 2];
+        const float gp = gx * x + gy * y + gz * z;
+        float nx = x - step * (gx - gp * x);
+        float ny = y - step * (gy - gp * y);
+        float nz = z - step * (gz - gp * z);
+        const float inv = rsqrtf(nx * nx + ny * ny + nz * nz);
+        px[i] = nx * inv;
+        py[i] = ny * inv;
+        pz[i] = nz * inv;
+    }
+}
+
+__global__ void philox_batch_kernel(const uint32_t *ctr, const uint32_t *key, uint32_t *out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint4 r = sn_philox(make_uint4(ctr[4 * i], ctr[4 * i + 1], ctr[4 * i + 2], ctr[4 * i + 3]),
+                              make_uint2(key[2 * i], key[2 * i + 1]));
+    out[4 * i + 0] = r.x;
+    out[4 * i + 1] = r.y;
+    out[4 * i + 2] = r.z;
+    out[4 * i + 3] = r.w;
+}
+
+__global__ void proposal_batch_kernel(const uint32_t *site, uint32_t sweep, uint2 key, int dim, int constrain,
+                                      float *out4, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 p;
+    float u;
+    if (!sn_proposal(site[i], sweep, SN_STREAM_SWEEP, key, dim, constrain, p, u))
+        p = make_float3(NAN, NAN, NAN);
+    out4[4 * i + 0] = p.x;
+    out4[4 * i + 1] = p.y;
+    out4[4 * i + 2] = p.z;
+    out4[4 * i + 3] = u;
+}
+
+int grid_for(long long n, int threads)
+{
+    long long g = (n + threads - 1) / threads;
+    if (g > 152LL * 32) g = 152LL * 32;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+cudaError_t sn_launch_init_lattice(const SnInitArgs &a, cudaStream_t st)
+{
+    init_lattice_kernel<<<grid_for(a.n, 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_upload_convert(const float *stage_xyz, const float *stage_len, float *px, float *py, float *pz,
+                                     float *len, long long n, float uniform_len, int mixed, float default_len,
+                                     int *flags, cudaStream_t st)
+{
+    upload_convert_kernel<<<grid_for(n, 256), 256, 0, st>>>(stage_xyz, stage_len, px, py, pz, len, n, uniform_len,
+                                                           mixed, default_len, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_download_convert(const float *px, const float *py, const float *pz, const float *len,
+                                       float *stage_xyz, float *stage_len, long long n, cudaStream_t st)
+{
+    download_convert_kernel<<<grid_for(n, 256), 256, 0, st>>>(px, py, pz, len, stage_xyz, stage_len, n);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnReplicaDev *reps, int nrep,
+                                uint32_t *sweep, SnExchange *ex, int *order, cudaStream_t st)
+{
+    sweep_end_kernel<<<1, 256, 0, st>>>(acc, state, hist, reps, nrep, sweep, ex, order);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
+                                       float cage, double *drift_max, int record, cudaStream_t st)
+{
+    recompute_finish_kernel<<<1, 1, 0, st>>>(red, state, reps, rep, cage, drift_max, record);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_quench_step(float *px, float *py, float *pz, const float *len, const float *grad,
+                                  long long n, float step, cudaStream_t st)
+{
+    quench_step_kernel<<<grid_for(n, 256), 256, 0, st>>>(px, py, pz, len, grad, n, step);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_philox_batch(const uint32_t *ctr, const uint32_t *key, uint32_t *out, int n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    philox_batch_kernel<<<(n + 255) / 256, 256, 0, st>>>(ctr, key, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_proposal_batch(const uint32_t *site, uint32_t sweep, uint32_t seed_lo, uint32_t seed_hi,
+                                     int dim, int constrain, float *out4, int n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    proposal_batch_kernel<<<(n + 255) / 256, 256, 0, st>>>(site, sweep, make_uint2(seed_lo, seed_hi), dim, constrain,
+                                                           out4, n);
+    return cudaGetLastError();
+}

@@ -1,0 +1,81 @@
+// sn_launch.h -- host-side entry points of the kernels, one set per cutoff
+// (sn_sweep_inst.cu is compiled once per cutoff with -DSN_RC=<rc>) plus the
+// small kernels of sn_kernels.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sn_internal.h"
+
+namespace sn_sweep {
+struct SnFieldArgs;
+}
+
+struct SnFieldArgsHost;
+
+typedef cudaError_t (*sn_sweep_launch_fn)(bool two_d, bool mixed, const SnPhaseArgs &a, int grid, int smem,
+                                          cudaStream_t st);
+typedef cudaError_t (*sn_field_launch_fn)(bool fp64, bool two_d, bool mixed, const void *field_args, int grid,
+                                          int smem, cudaStream_t st);
+typedef void (*sn_geo_fn)(bool two_d, int *S, int *SZ, int *NS, int *NF);
+
+#define SN_DECLARE_RC(N)                                                                                     \
+    cudaError_t sn_launch_sweep_rc##N(bool, bool, const SnPhaseArgs &, int, int, cudaStream_t);             \
+    cudaError_t sn_launch_field_rc##N(bool, bool, bool, const void *, int, int, cudaStream_t);             \
+    void sn_geo_rc##N(bool, int *, int *, int *, int *);
+SN_DECLARE_RC(1)
+SN_DECLARE_RC(2)
+SN_DECLARE_RC(3)
+SN_DECLARE_RC(4)
+SN_DECLARE_RC(5)
+SN_DECLARE_RC(6)
+
+// Field-pass arguments as the host fills them (layout identical to
+// sn_sweep::SnFieldArgs).
+struct SnFieldArgsHost {
+    const SnWork *work;
+    const SnReplicaDev *reps;
+    const SnTile *geoms;
+    float cage;
+    float K;
+    double *site_e;
+    float *grad;
+    double *red;
+    int red_stride;
+};
+
+// Exchange bookkeeping on the device.
+struct SnExchange {
+    int every;
+    int pad;
+    unsigned long long attempted;
+    unsigned long long accepted;
+    uint32_t seed_lo, seed_hi;
+};
+
+struct SnInitArgs {
+    float *px, *py, *pz, *len;
+    long long n;
+    int pattern;
+    int dim;
+    int n_species;
+    float dipoles[10];
+    float prevalence[10];
+    uint32_t seed_lo, seed_hi;
+};
+
+cudaError_t sn_launch_init_lattice(const SnInitArgs &a, cudaStream_t st);
+cudaError_t sn_launch_upload_convert(const float *stage_xyz, const float *stage_len, float *px, float *py, float *pz,
+                                     float *len, long long n, float uniform_len, int mixed, float default_len,
+                                     int *flags, cudaStream_t st);
+cudaError_t sn_launch_download_convert(const float *px, const float *py, const float *pz, const float *len,
+                                       float *stage_xyz, float *stage_len, long long n, cudaStream_t st);
+cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnReplicaDev *reps, int nrep,
+                                uint32_t *sweep, SnExchange *ex, int *order, cudaStream_t st);
+cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
+                                       float cage, double *drift_max, int record, cudaStream_t st);
+cudaError_t sn_launch_quench_step(float *px, float *py, float *pz, const float *len, const float *grad,
+                                  long long n, float step, cudaStream_t st);
+cudaError_t sn_launch_philox_batch(const uint32_t *ctr, const uint32_t *key, uint32_t *out, int n, cudaStream_t st);
+cudaError_t sn_launch_proposal_batch(const uint32_t *site, uint32_t sweep, uint32_t seed_lo, uint32_t seed_hi,
+                                     int dim, int constrain, float *out4, int n, cudaStream_t st);

@@ -1,0 +1,83 @@
+"""Build the CUDA library (``lib/libsn_gpu.so``) and the C host driver.
+
+nvcc compiles every translation unit for sm_103a only, in parallel: the
+sweep/field kernels once per cutoff (``-DSN_RC=1..6``), the small kernels,
+and the host side of the C ABI.  Outputs stay in-tree under
+``starrynight_gb300/lib/``.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(PKG, "csrc")
+LIBDIR = os.path.join(PKG, "lib")
+INCLUDE = os.path.join(os.path.dirname(PKG), "include")
+MAX_CUTOFF = 6
+
+NVCC = os.environ.get("NVCC", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+           "-I" + CSRC, "-I" + INCLUDE]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r
+
+
+def _deps():
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INCLUDE, "sn_gpu.h")]
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def lib_path() -> str:
+    return os.path.join(LIBDIR, "libsn_gpu.so")
+
+
+def driver_path() -> str:
+    return os.path.join(LIBDIR, "starrynight-gpu")
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    os.makedirs(LIBDIR, exist_ok=True)
+    deps = _deps()
+    so = lib_path()
+    if force or _stale(so, deps):
+        jobs = []
+        for rc in range(1, MAX_CUTOFF + 1):
+            obj = os.path.join(LIBDIR, "sn_sweep_rc%d.o" % rc)
+            jobs.append([NVCC] + ARCH + NVFLAGS + ["-DSN_RC=%d" % rc, "-c", os.path.join(CSRC, "sn_sweep_inst.cu"),
+                                                   "-o", obj])
+        for name in ("sn_kernels", "sn_gpu"):
+            jobs.append([NVCC] + ARCH + NVFLAGS + ["-c", os.path.join(CSRC, name + ".cu"),
+                                                   "-o", os.path.join(LIBDIR, name + ".o")])
+        with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            for r in ex.map(_run, jobs):
+                if verbose and (r.stdout or r.stderr):
+                    sys.stderr.write(r.stdout + r.stderr)
+        objs = [j[j.index("-o") + 1] for j in jobs]
+        tmp = so + ".tmp"
+        _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        os.replace(tmp, so)
+    drv = driver_path()
+    dsrc = [os.path.join(PKG, "driver", "starrynight-gpu.c"), os.path.join(PKG, "cfg", "libconfig_min.c")]
+    if all(os.path.exists(p) for p in dsrc) and (force or _stale(drv, dsrc + [so])):
+        _run(["gcc", "-O2", "-std=c11", "-Wall", "-I" + INCLUDE, "-I" + os.path.join(PKG, "cfg"), "-o", drv] + dsrc +
+             ["-L" + LIBDIR, "-lsn_gpu", "-Wl,-rpath,$ORIGIN", "-lm"])
+    return so
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

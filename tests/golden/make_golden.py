@@ -1,0 +1,144 @@
+"""Generate the golden fixtures in this directory from the UNMODIFIED
+reference sources (driven through ``oracle/_ref/libref_harness.so``, built by
+``make -C oracle ref`` where the reference tree is present).
+
+The reference ships no tests, golden vectors or fixtures, so these outputs of
+the reference itself are what pin the CPU oracle:
+
+  ref_neighbours.npz    gen_neighbour tables, cutoffs 1..6, 3D and Z == 1
+  ref_trajectories.npz  initial lattice (initialise_lattice_random +
+                        solid_solution) and the lattice after N MC_move calls,
+                        with ACCEPT/REJECT, for several parameter sets
+  ref_site_energy.npz   site_energy() values for random trial moves
+  ref_equilibrium.npz   per-sweep E/site and |P|/site of random-sequential runs
+                        (statistical oracle): 32^3, cutoff 3, CageStrain 1,
+                        T in {50,150,300,500}, 4 seeds each
+
+Usage:  python tests/golden/make_golden.py [--skip-equilibrium]
+"""
+from __future__ import annotations
+
+import multiprocessing as mp
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+TRAJ_CASES = [
+    dict(name="cube8", X=8, Y=8, Z=8, cutoff=3, T=300, moves=20000),
+    dict(name="field_K", X=6, Y=8, Z=10, cutoff=2, T=150, efield=(0.1, -0.2, 0.3), K=0.5, cage_strain=0.7,
+         moves=20000),
+    dict(name="slab", X=12, Y=12, Z=1, cutoff=3, T=300, moves=20000),
+    dict(name="constrain_x", X=8, Y=8, Z=8, cutoff=3, T=300, constrain_to_x=True, moves=20000),
+    dict(name="vacancies", X=8, Y=8, Z=8, cutoff=3, T=200, lengths=(1.0, 0.0), prevalence=(0.7, 0.3),
+         moves=20000),
+    dict(name="mixture_rc4", X=10, Y=10, Z=10, cutoff=4, T=250, lengths=(1.0, 0.5, 0.0),
+         prevalence=(0.5, 0.3, 0.2), efield=(0.0, 0.0, 0.2), moves=8000),
+]
+
+EQ_T = (50, 150, 300, 500)
+EQ_SEEDS = 4
+EQ_L = 32
+EQ_EQUIL = 300
+EQ_PROD = 200
+
+
+def _sim(R, c, seed=None):
+    return R.RefSim(c["X"], c["Y"], c["Z"], cutoff=c["cutoff"], cage_strain=c.get("cage_strain", 1.0),
+                    K=c.get("K", 0.0), efield=c.get("efield", (0.0, 0.0, 0.0)),
+                    constrain_to_x=c.get("constrain_to_x", False), T=c["T"],
+                    lengths=c.get("lengths", (1.0,)), prevalence=c.get("prevalence", (1.0,)), seed=seed)
+
+
+def neighbours(R):
+    out = {}
+    for rc in range(1, 7):
+        for Z in (8 * rc + 1, 1):
+            s = R.RefSim(4, 4, Z, cutoff=rc)
+            dxyz, d = s.neighbours()
+            tag = "rc%d_%s" % (rc, "2d" if Z == 1 else "3d")
+            out[tag + "_dxyz"] = dxyz
+            out[tag + "_d"] = d
+    np.savez_compressed(os.path.join(HERE, "ref_neighbours.npz"), **out)
+
+
+def trajectories(R):
+    out = {}
+    for c in TRAJ_CASES:
+        s = _sim(R, c)
+        out[c["name"] + "_init"] = s.lattice()
+        s.mc_moves(c["moves"])
+        out[c["name"] + "_final"] = s.lattice()
+        out[c["name"] + "_counts"] = np.array(s.counts(), np.uint64)
+        out[c["name"] + "_beta"] = np.array(s.beta())
+    np.savez_compressed(os.path.join(HERE, "ref_trajectories.npz"), **out)
+
+
+def site_energies(R):
+    c = dict(X=8, Y=8, Z=8, cutoff=3, T=300, efield=(0.05, 0.1, -0.2), K=0.4, cage_strain=1.3)
+    s = _sim(R, c)
+    s.mc_moves(5000)
+    lat = s.lattice()
+    rng = np.random.default_rng(2024)
+    n = 300
+    xyz = rng.integers(0, 8, size=(n, 3)).astype(np.int32)
+    v = rng.normal(size=(n, 3))
+    v = (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+    dE = np.array([s.site_energy(int(a), int(b), int(cc), v[i]) for i, (a, b, cc) in enumerate(xyz)])
+    np.savez_compressed(os.path.join(HERE, "ref_site_energy.npz"), lattice=lat, sites=xyz, new=v, dE=dE,
+                        params=np.array([8, 8, 8, 3, 300, 0.05, 0.1, -0.2, 0.4, 1.3]))
+
+
+def _eq_run(args):
+    T, k = args
+    from oracle import oracle as O
+    from oracle import ref_harness as R
+    L = EQ_L
+    seed = (0xDEADBEEF + T + 7919 * k) & 0xFFFFFFFF
+    s = R.RefSim(L, L, L, cutoff=3, T=T, seed=seed)
+    N = L ** 3
+    s.mc_moves(EQ_EQUIL * N)
+    m = O.make_model(L, L, L, 3, T=T)
+    E, P = [], []
+    for _ in range(EQ_PROD):
+        s.mc_moves(N)
+        lat = s.lattice()
+        px, py, pz, ln = O.soa(lat)
+        E.append(O.energy64(m, px, py, pz, ln)["E"] / N)
+        P.append(np.linalg.norm(lat[:, :3].astype(np.float64).sum(axis=0)) / N)
+    return T, k, np.array(E), np.array(P)
+
+
+def equilibrium():
+    jobs = [(T, k) for T in EQ_T for k in range(EQ_SEEDS)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(len(jobs), os.cpu_count() or 4)) as pool:
+        res = pool.map(_eq_run, jobs)
+    E = np.zeros((len(EQ_T), EQ_SEEDS, EQ_PROD))
+    P = np.zeros_like(E)
+    for T, k, e, p in res:
+        i = EQ_T.index(T)
+        E[i, k], P[i, k] = e, p
+    np.savez_compressed(os.path.join(HERE, "ref_equilibrium.npz"), T=np.array(EQ_T), E=E, P=P,
+                        L=EQ_L, equil=EQ_EQUIL, prod=EQ_PROD)
+
+
+def main():
+    from oracle import oracle as O
+    from oracle import ref_harness as R
+    O.build(ref=True)
+    if not R.available():
+        raise SystemExit("the reference harness is not built (reference tree missing?)")
+    neighbours(R)
+    trajectories(R)
+    site_energies(R)
+    if "--skip-equilibrium" not in sys.argv:
+        equilibrium()
+
+
+if __name__ == "__main__":
+    main()
