@@ -73,10 +73,16 @@ typedef struct sn_replica_desc {
 } sn_replica_desc;
 
 /* The block/colour schedule chosen for one replica (what the CPU oracle
- * mirrors).  A sweep visits block colours (cbx,cby,cbz) lexicographically;
- * inside a block colour it visits site colours (cx,cy,cz) lexicographically;
- * a site (x,y,z) belongs to block (x/bx, y/by, z/bz) of colour
- * (block mod m) and to site colour (local coordinate mod s). */
+ * mirrors).  A site (x,y,z) belongs to block (x/bx, y/by, z/bz) of block
+ * colour (block index mod m per axis) and to site colour (cx,cy,cz) =
+ * (local coordinate mod s).  A sweep visits block colours (cbx,cby,cbz)
+ * lexicographically; inside one it visits colour groups lexicographically
+ * by their representative (cx,cy,cz).  Without merging a group is one site
+ * colour.  With merge = 1 the representatives have cx < s/2 and a group is
+ * the pair c, c + (s/2,s/2,s/2) mod s: sites of the two colours are at least
+ * s/2 apart along every axis, farther than the cutoff, so they are updated
+ * together.  Sites updated together never interact, so the order inside a
+ * group does not matter. */
 typedef struct sn_schedule_info {
     int bx, by, bz;        /* block dimensions                          */
     int nbx, nby, nbz;     /* blocks per axis                           */
@@ -85,6 +91,8 @@ typedef struct sn_schedule_info {
     int halo;              /* halo width = cutoff (0 along z in 2D)     */
     int tile_slots;        /* shared-memory slots per tile (padded)     */
     int smem_bytes;        /* dynamic shared memory per block           */
+    int merge;             /* 1: colour pairs c, c + (s/2,s/2,s/2)      */
+    int threads;           /* threads per block of the sweep kernel     */
 } sn_schedule_info;
 
 /* Initial lattice patterns (InitialLattice, src/starrynight-main.c:184-203). */
@@ -220,6 +228,16 @@ int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *s
 sn_status sn_gpu_launch_count(const sn_handle *h, uint64_t *launches);
 /* The handle's CUDA stream as an opaque pointer (for event timing). */
 void *sn_gpu_stream(const sn_handle *h);
+/* Runs n_sweeps sweeps WITHOUT the graph, timing every block-colour launch
+ * of the sweep kernel with CUDA events on the handle's stream:
+ * *avg_launch_ms = mean duration of one launch, *avg_sweep_ms = mean sweep.
+ * The sweeps are real (they advance the lattice and the sweep counter). */
+sn_status sn_gpu_phase_times(sn_handle *h, int n_sweeps, double *avg_launch_ms, double *avg_sweep_ms,
+                             int *launches_per_sweep);
+/* Measured FP32 FMA throughput of the current device (TFLOP/s, an FMA
+ * counted as 2) and its nominal maximum SM clock; the roofline denominator
+ * for the sweep kernel, which runs on CUDA cores. */
+sn_status sn_gpu_fp32_peak(double *tflops, double *sm_clock_mhz);
 /* Number of neighbour offsets (gen_neighbour's count) for a cutoff. */
 int sn_neighbour_count(int cutoff, int Z);
 

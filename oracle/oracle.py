@@ -55,7 +55,7 @@ class Schedule(ctypes.Structure):
         ("bx", ctypes.c_int), ("by", ctypes.c_int), ("bz", ctypes.c_int),
         ("nbx", ctypes.c_int), ("nby", ctypes.c_int), ("nbz", ctypes.c_int),
         ("mx", ctypes.c_int), ("my", ctypes.c_int), ("mz", ctypes.c_int),
-        ("s", ctypes.c_int),
+        ("s", ctypes.c_int), ("merge", ctypes.c_int),
     ]
 
 
@@ -181,8 +181,8 @@ def ref_site_energy(m: Model, lat4: np.ndarray, x: int, y: int, z: int, new4) ->
 
 def make_schedule(d: dict) -> Schedule:
     s = Schedule()
-    for k in ("bx", "by", "bz", "nbx", "nby", "nbz", "mx", "my", "mz", "s"):
-        setattr(s, k, int(d[k]))
+    for k in ("bx", "by", "bz", "nbx", "nby", "nbz", "mx", "my", "mz", "s", "merge"):
+        setattr(s, k, int(d.get(k, 0)))
     return s
 
 

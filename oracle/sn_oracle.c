@@ -483,13 +483,19 @@ uint64_t sno_colour_sweep(const sno_model *m, const sno_schedule *sc, const sno_
     if (margin_out)
         for (long i = 0; i < N; i++) margin_out[i] = NAN;
     if (accept_out) memset(accept_out, 0, (size_t)N);
+    /* colour groups: representative (gx,gy,gz) and, when merged, the
+     * partner shifted by s/2 along every axis (the two never interact) */
     for (cbx = 0; cbx < sc->mx; cbx++)
         for (cby = 0; cby < sc->my; cby++)
             for (cbz = 0; cbz < sc->mz; cbz++)
-                for (cx = 0; cx < sc->s; cx++)
-                    for (cy = 0; cy < sc->s; cy++)
-                        for (cz = 0; cz < szc; cz++) {
+                for (int gx = 0; gx < (sc->merge ? sc->s / 2 : sc->s); gx++)
+                    for (int gy = 0; gy < sc->s; gy++)
+                        for (int gz = 0; gz < szc; gz++)
+                            for (int half = 0; half < (sc->merge ? 2 : 1); half++) {
                             int ibx, iby, ibz;
+                            cx = half ? (gx + sc->s / 2) % sc->s : gx;
+                            cy = half ? (gy + sc->s / 2) % sc->s : gy;
+                            cz = half ? (gz + sc->s / 2) % sc->s : gz;
                             for (ibx = cbx; ibx < sc->nbx; ibx += sc->mx)
                                 for (iby = cby; iby < sc->nby; iby += sc->my)
                                     for (ibz = cbz; ibz < sc->nbz; ibz += sc->mz) {

@@ -82,6 +82,7 @@ typedef struct {
     int nbx, nby, nbz;   /* blocks per axis */
     int mx, my, mz;      /* block colours per axis */
     int s;               /* site-colour stride (cutoff + 1) */
+    int merge;           /* 1: colours c and c + (s/2,s/2,s/2) form one group */
 } sno_schedule;
 
 typedef struct {

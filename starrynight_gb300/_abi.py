@@ -49,7 +49,7 @@ class ReplicaDesc(ctypes.Structure):
 
 class ScheduleInfo(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in ("bx", "by", "bz", "nbx", "nby", "nbz", "mx", "my", "mz", "s",
-                                             "halo", "tile_slots", "smem_bytes")]
+                                             "halo", "tile_slots", "smem_bytes", "merge", "threads")]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -105,6 +105,8 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_stream": ([h], _vp),
             "sn_neighbour_count": ([_i, _i], _i),
             "sn_gpu_philox": ([_vp, _vp, _vp, _i], _i),
+            "sn_gpu_fp32_peak": ([_P(ctypes.c_double), _P(ctypes.c_double)], _i),
+            "sn_gpu_phase_times": ([h, _i, _P(ctypes.c_double), _P(ctypes.c_double), _P(_i)], _i),
             "sn_gpu_proposals": ([h, _i, _vp, _i, ctypes.c_uint32, _vp], _i),
         }
         for name, (args, res) in sig.items():

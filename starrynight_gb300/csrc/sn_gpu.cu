@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -37,6 +38,9 @@ const sn_geo_fn k_geo[SN_MAX_CUTOFF + 1] = {nullptr,     sn_geo_rc1, sn_geo_rc2,
                                             sn_geo_rc4,  sn_geo_rc5, sn_geo_rc6};
 
 const int kSmemLimit = 227 * 1024;
+// per-block shared memory that still lets two blocks share an SM (228 KB per
+// SM, 1 KB reserved per block)
+const int kSmemTwoPerSm = (228 * 1024 - 2 * 1024) / 2;
 
 thread_local std::string g_last_error;
 
@@ -57,11 +61,15 @@ void axis_starts(int T, int S, int *start)
 int pi_host(const int *start, int S, int u) { return start[u % S] + u / S; }
 
 // Sum over site colours and warps of the worst bank multiplicity of the
-// targets' slots (32 lanes -> 32 banks is the ideal: cost 1 per warp).
+// targets' slots (32 lanes -> 32 banks is the ideal: cost 1 per warp).  A
+// slot is 3 words, so distinct slots mod 32 are distinct banks.
+// Lane t of a colour is target (qx,qy,qz) = t unravelled over nq (z
+// fastest); lanes beyond the colour's own target count are idle.
 long long conflict_cost(const SnTile &t, int S, bool two_d, int Sy, int Sx)
 {
     long long cost = 0;
     const int SZ = two_d ? 1 : S;
+    const int ntp = t.nq[0] * t.nq[1] * t.nq[2];
     int cnt[32];
     for (int cx = 0; cx < S; cx++)
         for (int cy = 0; cy < S; cy++)
@@ -69,19 +77,18 @@ long long conflict_cost(const SnTile &t, int S, bool two_d, int Sy, int Sx)
                 const int nx = cx < t.B[0] ? ceil_div(t.B[0] - cx, S) : 0;
                 const int ny = cy < t.B[1] ? ceil_div(t.B[1] - cy, S) : 0;
                 const int nz = two_d ? 1 : (cz < t.B[2] ? ceil_div(t.B[2] - cz, S) : 0);
-                const int nt = nx * ny * nz;
-                if (!nt) continue;
+                if (!(nx && ny && nz)) continue;
                 const int bx0 = pi_host(t.start[0], S, cx + t.H[0]);
                 const int by0 = pi_host(t.start[1], S, cy + t.H[1]);
-                const int bz0 = two_d ? 0 : pi_host(t.start[2], S, cz + t.H[2]);
-                for (int w0 = 0; w0 < nt; w0 += 32) {
+                const int bz0 = two_d ? 0 : cz + t.H[2];  // z stored plainly
+                for (int w0 = 0; w0 < ntp; w0 += 32) {
                     memset(cnt, 0, sizeof(cnt));
                     int worst = 0;
-                    for (int t_ = w0; t_ < std::min(nt, w0 + 32); t_++) {
-                        const int qz = t_ % nz, r = t_ / nz, qy = r % ny, qx = r / ny;
-                        const long long slot = (long long)(bx0 + qx) * Sx + (long long)(by0 + qy) * Sy + bz0 + qz;
-                        const int b = (int)(slot & 31);
-                        worst = std::max(worst, ++cnt[b]);
+                    for (int q = w0; q < std::min(ntp, w0 + 32); q++) {
+                        const int qz = q % t.nq[2], qy = (q / t.nq[2]) % t.nq[1], qx = q / (t.nq[2] * t.nq[1]);
+                        if (qx >= nx || qy >= ny || qz >= nz) continue;
+                        const long long slot = (long long)(bx0 + qx) * Sx + (long long)(by0 + qy) * Sy + bz0 + S * qz;
+                        worst = std::max(worst, ++cnt[(int)(slot & 31)]);
                     }
                     cost += worst;
                 }
@@ -111,8 +118,8 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
         return false;
     }
     const bool two_d = (Z == 1);
-    int S, SZ, NS, NF;
-    k_geo[rc](two_d, &S, &SZ, &NS, &NF);
+    int S, SZ, NS, NF, merge;
+    k_geo[rc](two_d, &S, &SZ, &NS, &NF, &merge);
     const int L[3] = {X, Y, Z};
     std::vector<int> cands[3];
     for (int a = 0; a < 3; a++) {
@@ -133,63 +140,89 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
         int balanced;
     };
     std::vector<Cand> all;
+    // SN_BLOCK="bx,by,bz" forces a block shape (for tuning); it must be valid
+    int force[3] = {0, 0, 0};
+    if (const char *env = getenv("SN_BLOCK")) {
+        if (sscanf(env, "%d,%d,%d", &force[0], &force[1], &force[2]) != 3) force[0] = 0;
+    }
     for (int bx : cands[0])
         for (int by : cands[1])
             for (int bz : cands[2]) {
+                if (force[0] && (bx != force[0] || by != force[1] || bz != force[2])) continue;
                 Cand c{{bx, by, bz}, (long long)bx * by * bz, 0};
                 c.balanced = (bx % S == 0) + (by % S == 0) + (two_d || bz % S == 0);
                 all.push_back(c);
             }
-    // Largest blocks first (least halo per site), balanced colours first,
-    // then the most cubic.
-    std::sort(all.begin(), all.end(), [](const Cand &a, const Cand &b) {
+    // Largest blocks first, then the smallest tile (least halo per site),
+    // balanced colours, and longer z and y extents (contiguous rows).
+    auto tile_sites = [&](const Cand &c) {
+        return (long long)(c.B[0] + 2 * rc) * (c.B[1] + 2 * rc) * (two_d ? 1 : c.B[2] + 2 * rc);
+    };
+    std::sort(all.begin(), all.end(), [&](const Cand &a, const Cand &b) {
         if (a.vol != b.vol) return a.vol > b.vol;
+        if (tile_sites(a) != tile_sites(b)) return tile_sites(a) < tile_sites(b);
         if (a.balanced != b.balanced) return a.balanced > b.balanced;
-        const int sa = std::max({a.B[0], a.B[1], a.B[2]}) - std::min({a.B[0], a.B[1], a.B[2]});
-        const int sb = std::max({b.B[0], b.B[1], b.B[2]}) - std::min({b.B[0], b.B[1], b.B[2]});
-        return sa < sb;
+        if (a.B[2] != b.B[2]) return a.B[2] > b.B[2];
+        return a.B[1] > b.B[1];
     });
-    for (const Cand &c : all) {
-        SnTile t;
-        memset(&t, 0, sizeof(t));
-        for (int a = 0; a < 3; a++) {
-            t.B[a] = c.B[a];
-            t.H[a] = (a == 2 && two_d) ? 0 : rc;
-            t.T[a] = (a == 2 && two_d) ? 1 : c.B[a] + 2 * rc;
-            t.nb[a] = L[a] / c.B[a];
-            t.m[a] = (a == 2 && two_d) ? 1 : 2;
-            axis_starts(t.T[a], S, t.start[a]);
-        }
-        t.maxt = ceil_div(t.B[0], S) * ceil_div(t.B[1], S) * (two_d ? 1 : ceil_div(t.B[2], S));
-        // quick lower bound on shared memory with no padding
-        {
-            const sn_sweep::Carve cv =
-                sn_sweep::sn_carve(t.T[0] * t.T[1] * t.T[2], t.maxt, S, SZ, NS, NF, mixed);
-            if ((int)cv.total > kSmemLimit) continue;
-        }
-        long long best = -1;
-        int bSy = 0, bSx = 0;
-        for (int dy = 0; dy < 32; dy++) {
-            const int Sy = t.T[2] + dy;
-            for (int dx = 0; dx < 32; dx++) {
-                const int Sx = t.T[1] * Sy + dx;
-                const sn_sweep::Carve cv = sn_sweep::sn_carve(Sx * t.T[0], t.maxt, S, SZ, NS, NF, mixed);
-                if ((int)cv.total > kSmemLimit) continue;
-                const long long cost = conflict_cost(t, S, two_d, Sy, Sx);
-                if (best < 0 || cost < best) {
-                    best = cost;
-                    bSy = Sy;
-                    bSx = Sx;
+    const int nh = merge ? 2 : 1;
+    const int ng = (merge ? S / 2 : S) * S * SZ;
+    // Pass 0 looks for shapes that fit two blocks per SM (each block's
+    // barriers then overlap the other's work: measured faster at 256^3);
+    // pass 1 takes the largest shape that fits one block per SM.
+    for (int pass = 0; pass < 2; pass++) {
+        const int limit = pass == 0 ? kSmemTwoPerSm : kSmemLimit;
+        for (const Cand &c : all) {
+            SnTile t;
+            memset(&t, 0, sizeof(t));
+            for (int a = 0; a < 3; a++) {
+                t.B[a] = c.B[a];
+                t.H[a] = (a == 2 && two_d) ? 0 : rc;
+                t.T[a] = (a == 2 && two_d) ? 1 : c.B[a] + 2 * rc;
+                t.nb[a] = L[a] / c.B[a];
+                t.m[a] = (a == 2 && two_d) ? 1 : 2;
+                t.nq[a] = (a == 2 && two_d) ? 1 : ceil_div(c.B[a], S);
+                axis_starts(t.T[a], S, t.start[a]);
+            }
+            t.tp = ceil_div(t.nq[0] * t.nq[1] * t.nq[2], 32) * 32;
+            t.tg = nh * t.tp;
+            t.threads = NS * t.tg;
+            t.ng = ng;
+            t.merge = merge;
+            if (t.threads > (pass == 0 ? SN_MAX_THREADS / 2 : SN_MAX_THREADS)) continue;
+            const int pc_min = pass == 0 ? std::min(8, ng) : 1;
+            // quick lower bound on shared memory with no padding
+            if ((int)sn_sweep::sn_carve(t.T[0] * t.T[1] * t.T[2], t.tg, pc_min, NS, S, NF, mixed, 4).total > limit)
+                continue;
+            long long best = -1;
+            int bSy = 0, bSx = 0;
+            for (int dy = 0; dy < 32; dy++) {
+                const int Sy = t.T[2] + dy;
+                for (int dx = 0; dx < 32; dx++) {
+                    const int Sx = t.T[1] * Sy + dx;
+                    if ((int)sn_sweep::sn_carve(Sx * t.T[0], t.tg, pc_min, NS, S, NF, mixed, 4).total > limit)
+                        continue;
+                    const long long cost = conflict_cost(t, S, two_d, Sy, Sx);
+                    if (best < 0 || cost < best) {
+                        best = cost;
+                        bSy = Sy;
+                        bSx = Sx;
+                    }
                 }
             }
+            if (best < 0) continue;
+            t.Sy = bSy;
+            t.Sx = bSx;
+            t.slots = bSx * t.T[0];
+            // stage as many groups' proposals at once as the budget allows
+            t.pc = ng;
+            while (t.pc > 1 && (int)sn_sweep::sn_carve(t.slots, t.tg, t.pc, NS, S, NF, mixed, 4).total > limit) t.pc--;
+            t.smem_bytes = (int)sn_sweep::sn_carve(t.slots, t.tg, t.pc, NS, S, NF, mixed, 4).total;
+            t.field_smem = (int)sn_sweep::sn_carve(t.slots, t.tg, 0, NS, S, NF, mixed, 8).total;
+            if (t.smem_bytes > limit || t.field_smem > kSmemLimit || t.pc < pc_min) continue;
+            out = t;
+            return true;
         }
-        if (best < 0) continue;
-        t.Sy = bSy;
-        t.Sx = bSx;
-        t.slots = bSx * t.T[0];
-        t.smem_bytes = (int)sn_sweep::sn_carve(t.slots, t.maxt, S, SZ, NS, NF, mixed).total;
-        out = t;
-        return true;
     }
     why = "no block shape fits in shared memory for this lattice and cutoff";
     return false;
@@ -210,6 +243,8 @@ void fill_info(const SnTile &t, int rc, sn_schedule_info *o)
     o->halo = rc;
     o->tile_slots = t.slots;
     o->smem_bytes = t.smem_bytes;
+    o->merge = t.merge;
+    o->threads = t.threads;
 }
 
 }  // namespace
@@ -239,7 +274,7 @@ struct sn_handle {
     int *d_order = nullptr;
     int *d_flags = nullptr;
     SnWork *d_work = nullptr;
-    std::vector<int> work_off, work_cnt, work_smem;  // [phase*2 + variant]
+    std::vector<int> work_off, work_cnt, work_smem, work_thr;  // [phase*2 + variant]
     std::vector<int> fwork_off, fwork_cnt;           // per replica, all blocks
     std::vector<float *> lattice_mem;
     // scratch (lazy)
@@ -321,7 +356,8 @@ SnFieldArgsHost field_args(sn_handle *h, int r, double *site_e, float *grad, dou
 sn_status launch_field(sn_handle *h, int r, bool fp64, const SnFieldArgsHost &a)
 {
     const bool two_d = h->desc[r].Z == 1;
-    SN_CK(h, k_field[h->rc](fp64, two_d, h->mixed, &a, h->fwork_cnt[r], h->tiles[r].smem_bytes, h->stream));
+    SN_CK(h, k_field[h->rc](fp64, two_d, h->mixed, &a, h->fwork_cnt[r], h->tiles[r].threads, h->tiles[r].field_smem,
+                            h->stream));
     h->launches++;
     return SN_OK;
 }
@@ -340,14 +376,12 @@ sn_status recompute_one(sn_handle *h, int r, int prec, int record)
     return SN_OK;
 }
 
-sn_status capture_graph(sn_handle *h)
+// Issue one sweep's kernels on the handle's stream.  With events (2 per
+// launch), each block-colour launch is bracketed for timing.
+cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> *events)
 {
-    // configure function attributes outside the capture
-    for (int v = 0; v < 2; v++) SN_CK(h, k_sweep[h->rc](v == 1, h->mixed, SnPhaseArgs{}, 0, 0, h->stream));
-    cudaGraph_t g;
-    SN_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    uint64_t nodes = 0;
     cudaError_t e = cudaSuccess;
+    size_t ev = 0;
     for (int p = 0; p < 8 && e == cudaSuccess; p++)
         for (int v = 0; v < 2 && e == cudaSuccess; v++) {
             const int k = p * 2 + v;
@@ -363,14 +397,27 @@ sn_status capture_graph(sn_handle *h)
             a.K = h->params.K;
             a.constrain = h->params.constrain_to_x;
             a.dim = h->params.dim;
-            e = k_sweep[h->rc](v == 1, h->mixed, a, h->work_cnt[k], h->work_smem[k], h->stream);
-            nodes++;
+            if (events && ev + 1 < events->size()) e = cudaEventRecord((*events)[ev++], h->stream);
+            if (e == cudaSuccess) e = k_sweep[h->rc](v == 1, h->mixed, a, h->work_cnt[k], h->work_thr[k], h->work_smem[k], h->stream);
+            if (events && ev < events->size() && e == cudaSuccess) e = cudaEventRecord((*events)[ev++], h->stream);
+            if (nodes) (*nodes)++;
         }
     if (e == cudaSuccess) {
         e = sn_launch_sweep_end(h->d_acc, h->d_state, h->d_hist, h->d_reps, h->nrep, h->d_sweep, h->d_ex, h->d_order,
                                 h->stream);
-        nodes++;
+        if (nodes) (*nodes)++;
     }
+    return e;
+}
+
+sn_status capture_graph(sn_handle *h)
+{
+    // configure function attributes outside the capture
+    for (int v = 0; v < 2; v++) SN_CK(h, k_sweep[h->rc](v == 1, h->mixed, SnPhaseArgs{}, 0, 0, 0, h->stream));
+    cudaGraph_t g;
+    SN_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    uint64_t nodes = 0;
+    cudaError_t e = issue_sweep(h, &nodes, nullptr);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
     if (e != cudaSuccess) return fail(h, SN_ERR_CUDA, "sweep capture: %s", cudaGetErrorString(e));
     if (e2 != cudaSuccess) return fail(h, SN_ERR_CUDA, "sweep capture end: %s", cudaGetErrorString(e2));
@@ -451,11 +498,19 @@ int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *s
     const bool two_d = Z == 1;
     if (sc->bx * sc->nbx != X || sc->by * sc->nby != Y || sc->bz * sc->nbz != Z) return 0;
     if (sc->nbx % sc->mx || sc->nby % sc->my || sc->nbz % sc->mz) return 0;
+    if (sc->merge && (two_d || sc->s % 2)) return 0;
+    // key = (block colour, colour group); a group is one site colour, or the
+    // pair c, c + (s/2,s/2,s/2) when merged
     auto key = [&](int x, int y, int z) {
         const int bx = x / sc->bx, by = y / sc->by, bz = z / sc->bz;
-        const int lx = x % sc->bx, ly = y % sc->by, lz = z % sc->bz;
+        int cx = (x % sc->bx) % sc->s, cy = (y % sc->by) % sc->s, cz = two_d ? 0 : (z % sc->bz) % sc->s;
+        if (sc->merge && cx >= sc->s / 2) {
+            cx -= sc->s / 2;
+            cy = (cy + sc->s / 2) % sc->s;
+            cz = (cz + sc->s / 2) % sc->s;
+        }
         long long k = ((bx % sc->mx) * sc->my + (by % sc->my)) * (long long)sc->mz + (bz % sc->mz);
-        k = ((k * sc->s + lx % sc->s) * sc->s + ly % sc->s) * sc->s + (two_d ? 0 : lz % sc->s);
+        k = ((k * sc->s + cx) * sc->s + cy) * sc->s + cz;
         return k;
     };
     const int zc = two_d ? 0 : cutoff;
@@ -522,6 +577,7 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     h->work_off.assign(16, 0);
     h->work_cnt.assign(16, 0);
     h->work_smem.assign(16, 0);
+    h->work_thr.assign(16, 0);
     h->fwork_off.assign(n_replicas, 0);
     h->fwork_cnt.assign(n_replicas, 0);
 
@@ -583,6 +639,7 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
                             if (bx % t.m[0] != cb[0] || by % t.m[1] != cb[1] || bz % t.m[2] != cb[2]) continue;
                             work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
                             h->work_smem[k] = std::max(h->work_smem[k], t.smem_bytes);
+                            h->work_thr[k] = std::max(h->work_thr[k], t.threads);
                         }
             }
             h->work_cnt[k] = (int)work.size() - h->work_off[k];
@@ -1013,6 +1070,79 @@ sn_status sn_gpu_launch_count(const sn_handle *h, uint64_t *launches)
 }
 
 void *sn_gpu_stream(const sn_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+sn_status sn_gpu_phase_times(sn_handle *h, int n_sweeps, double *avg_launch_ms, double *avg_sweep_ms,
+                             int *launches_per_sweep)
+{
+    if (!h || n_sweeps < 1) return fail(h, SN_ERR_ARG, "need a handle and n_sweeps >= 1");
+    int nl = 0;
+    for (int k = 0; k < 16; k++) nl += h->work_cnt[k] ? 1 : 0;
+    std::vector<cudaEvent_t> ev(2 * (size_t)nl);
+    for (auto &x : ev) SN_CK(h, cudaEventCreate(&x));
+    cudaEvent_t s0, s1;
+    SN_CK(h, cudaEventCreate(&s0));
+    SN_CK(h, cudaEventCreate(&s1));
+    double tot_launch = 0.0, tot_sweep = 0.0;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < n_sweeps && e == cudaSuccess; i++) {
+        e = cudaEventRecord(s0, h->stream);
+        if (e == cudaSuccess) e = issue_sweep(h, nullptr, &ev);
+        if (e == cudaSuccess) e = cudaEventRecord(s1, h->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(s1);
+        for (int k = 0; k < nl && e == cudaSuccess; k++) {
+            float ms = 0.0f;
+            e = cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]);
+            tot_launch += ms;
+        }
+        float sw = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&sw, s0, s1);
+        tot_sweep += sw;
+        h->launches += (uint64_t)nl + 1;
+        h->sweeps++;
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    cudaEventDestroy(s0);
+    cudaEventDestroy(s1);
+    if (e != cudaSuccess) return fail(h, SN_ERR_CUDA, "phase timing: %s", cudaGetErrorString(e));
+    if (avg_launch_ms) *avg_launch_ms = tot_launch / ((double)n_sweeps * nl);
+    if (avg_sweep_ms) *avg_sweep_ms = tot_sweep / n_sweeps;
+    if (launches_per_sweep) *launches_per_sweep = nl;
+    return SN_OK;
+}
+
+sn_status sn_gpu_fp32_peak(double *tflops, double *sm_clock_mhz)
+{
+    if (!tflops) return fail(nullptr, SN_ERR_ARG, "null output");
+    int dev = 0, nsm = 0, clk = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return fail(nullptr, SN_ERR_CUDA, "no CUDA device");
+    cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, dev);
+    const int threads = 1024, blocks = nsm * 2, iters = 1 << 16;
+    float *d = nullptr;
+    if (cudaMalloc(&d, (size_t)blocks * threads * sizeof(float)) != cudaSuccess)
+        return fail(nullptr, SN_ERR_NOMEM, "cudaMalloc failed");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t e = sn_launch_fma_peak(d, blocks, threads, iters / 16, 0);  // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 5 && e == cudaSuccess; rep++) {
+        cudaEventRecord(e0, 0);
+        e = sn_launch_fma_peak(d, blocks, threads, iters, 0);
+        cudaEventRecord(e1, 0);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms > 0.0f && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(nullptr, SN_ERR_CUDA, "fma probe: %s", cudaGetErrorString(e));
+    *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
+    if (sm_clock_mhz) *sm_clock_mhz = clk / 1000.0;
+    return SN_OK;
+}
 
 sn_status sn_gpu_philox(const uint32_t *ctr, const uint32_t *key, uint32_t *out, int n)
 {

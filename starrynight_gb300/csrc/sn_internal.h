@@ -9,15 +9,15 @@
 
 #include <cstdint>
 
-#define SN_THREADS 256           // threads per sweep block
+#define SN_MAX_THREADS 512       // largest sweep / field block
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log
 
 // Geometry of one replica's tiles: block dims, tile dims (block + halo),
-// and the per-axis permutation that stores each axis class-major
+// and the permutation that stores the x and y axes class-major
 // (coordinates u with the same u mod s contiguous).  Slot of tile
-// coordinate (ux,uy,uz) = pi_x(ux)*Sx + pi_y(uy)*Sy + pi_z(uz), with
-// pi_a(u) = start[a][u mod s] + u / s.
+// coordinate (ux,uy,uz) = pi_x(ux)*Sx + pi_y(uy)*Sy + uz, with
+// pi_a(u) = start[a][u mod s] + u / s; z is stored plainly.
 struct SnTile {
     int B[3];        // block dims
     int T[3];        // tile dims = B + 2*halo (z: 1 in 2D)
@@ -26,9 +26,16 @@ struct SnTile {
     int m[3];        // block colours per axis
     int Sy, Sx;      // padded slot strides (z stride is 1)
     int slots;       // Sx * T[0]
-    int maxt;        // max targets of one site colour inside a block
+    int nq[3];       // targets per axis of the fullest site colour: ceil(B/s)
+    int tp;          // targets of one site colour, padded to a warp multiple
+    int tg;          // targets of one colour group (1 or 2 colours)
+    int ng;          // colour groups per block
+    int pc;          // colour groups whose proposals are staged at once
+    int threads;     // sweep / field kernel block size (splits * tg)
+    int merge;       // 1: colours c and c + (s/2,s/2,s/2) are updated together
     int start[3][SN_MAX_S];
     int smem_bytes;  // dynamic shared memory for the sweep kernel
+    int field_smem;  // dynamic shared memory for the field kernel
 };
 
 struct SnReplicaDev {

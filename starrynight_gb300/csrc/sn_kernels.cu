@@ -202,6 +202,23 @@ __global__ void proposal_batch_kernel(const uint32_t *site, uint32_t sweep, uint
     out4[4 * i + 3] = u;
 }
 
+// FP32 FMA throughput probe: 8 independent chains per thread, no memory
+// traffic in the loop; one result per thread keeps the work live.
+__global__ void fma_peak_kernel(float *out, int iters, float a, float b)
+{
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = (float)(threadIdx.x + k) * 1e-3f;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = fmaf(v[k], a, b);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += v[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 int grid_for(long long n, int threads)
 {
     long long g = (n + threads - 1) / threads;
@@ -259,6 +276,12 @@ cudaError_t sn_launch_philox_batch(const uint32_t *ctr, const uint32_t *key, uin
 {
     if (n <= 0) return cudaSuccess;
     philox_batch_kernel<<<(n + 255) / 256, 256, 0, st>>>(ctr, key, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_fma_peak(float *out, int blocks, int threads, int iters, cudaStream_t st)
+{
+    fma_peak_kernel<<<blocks, threads, 0, st>>>(out, iters, 0.999999f, 1e-6f);
     return cudaGetLastError();
 }
 

@@ -13,16 +13,16 @@ struct SnFieldArgs;
 
 struct SnFieldArgsHost;
 
-typedef cudaError_t (*sn_sweep_launch_fn)(bool two_d, bool mixed, const SnPhaseArgs &a, int grid, int smem,
-                                          cudaStream_t st);
-typedef cudaError_t (*sn_field_launch_fn)(bool fp64, bool two_d, bool mixed, const void *field_args, int grid,
+typedef cudaError_t (*sn_sweep_launch_fn)(bool two_d, bool mixed, const SnPhaseArgs &a, int grid, int threads,
                                           int smem, cudaStream_t st);
-typedef void (*sn_geo_fn)(bool two_d, int *S, int *SZ, int *NS, int *NF);
+typedef cudaError_t (*sn_field_launch_fn)(bool fp64, bool two_d, bool mixed, const void *field_args, int grid,
+                                          int threads, int smem, cudaStream_t st);
+typedef void (*sn_geo_fn)(bool two_d, int *S, int *SZ, int *NS, int *NF, int *merge);
 
 #define SN_DECLARE_RC(N)                                                                                     \
-    cudaError_t sn_launch_sweep_rc##N(bool, bool, const SnPhaseArgs &, int, int, cudaStream_t);             \
-    cudaError_t sn_launch_field_rc##N(bool, bool, bool, const void *, int, int, cudaStream_t);             \
-    void sn_geo_rc##N(bool, int *, int *, int *, int *);
+    cudaError_t sn_launch_sweep_rc##N(bool, bool, const SnPhaseArgs &, int, int, int, cudaStream_t);        \
+    cudaError_t sn_launch_field_rc##N(bool, bool, bool, const void *, int, int, int, cudaStream_t);        \
+    void sn_geo_rc##N(bool, int *, int *, int *, int *, int *);
 SN_DECLARE_RC(1)
 SN_DECLARE_RC(2)
 SN_DECLARE_RC(3)
@@ -76,6 +76,7 @@ cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const 
                                        float cage, double *drift_max, int record, cudaStream_t st);
 cudaError_t sn_launch_quench_step(float *px, float *py, float *pz, const float *len, const float *grad,
                                   long long n, float step, cudaStream_t st);
+cudaError_t sn_launch_fma_peak(float *out, int blocks, int threads, int iters, cudaStream_t st);
 cudaError_t sn_launch_philox_batch(const uint32_t *ctr, const uint32_t *key, uint32_t *out, int n, cudaStream_t st);
 cudaError_t sn_launch_proposal_batch(const uint32_t *site, uint32_t sweep, uint32_t seed_lo, uint32_t seed_hi,
                                      int dim, int constrain, float *out4, int n, cudaStream_t st);

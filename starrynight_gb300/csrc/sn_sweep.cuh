@@ -13,7 +13,7 @@
 // over X*Y*Z steps (src/starrynight-montecarlo-core.c:143-191), in a
 // different but fixed order.
 //
-// Per site colour:
+// Per site-colour group (one colour, or two colours that cannot interact):
 //   1. (split) NS warp groups each sum a slice of the cutoff stencil into
 //      partial local fields h = sum T_o p_j and nearest-neighbour sums
 //      nn = sum_{|o|=1} p_j; T_o = (I - 3 n n^T)/d^3 is a compile-time
@@ -45,7 +45,16 @@ struct Geo {
     static constexpr int SZ = TWO_D ? 1 : S;         // site colours along z
     static constexpr int NF = 2 * RC + 1;            // offsets per axis
     static constexpr int NP = sn_stencil::npairs(RC, TWO_D);
-    static constexpr int NS = (NP + 7) / 15 < 1 ? 1 : ((NP + 7) / 15 > 16 ? 16 : (NP + 7) / 15);
+    // neighbour-list splits: about 15 +-o pairs per thread, at most 8
+    static constexpr int NS = (NP + 7) / 15 < 1 ? 1 : ((NP + 7) / 15 > 8 ? 8 : (NP + 7) / 15);
+    // Site colours c and c + (s/2, s/2, s/2) never interact when every
+    // component of the displacement between their sites is >= s/2, i.e. when
+    // 3 (s/2)^2 > cutoff^2 (cutoff 1, 3, 5 in 3D).  They are then updated
+    // together, halving the number of sequential sub-phases.
+    static constexpr bool MERGE = !TWO_D && (S % 2 == 0) && 3 * (S / 2) * (S / 2) > RC * RC;
+    static constexpr int NH = MERGE ? 2 : 1;         // colours per group
+    static constexpr int HX = MERGE ? S / 2 : S;     // representative colours along x
+    static constexpr int NG = HX * S * SZ;           // colour groups per block
 };
 
 __device__ __forceinline__ float sn_fma(float a, float b, float c) { return fmaf(a, b, c); }
@@ -56,17 +65,20 @@ __device__ __forceinline__ double sn_fma(double a, double b, double c) { return 
 template <typename R, int RC, bool TWO_D, bool MIXED, int I>
 __device__ __forceinline__ void pair_step(const unsigned char *__restrict__ base, uint32_t tb,
                                           const int (&FX)[2 * RC + 1], const int (&FY)[2 * RC + 1],
-                                          const int (&FZ)[2 * RC + 1], const float *__restrict__ tlen,
-                                          uint32_t tslot, R (&h)[2][3], R (&nn)[3])
+                                          const float *__restrict__ tlen, uint32_t tslot, R (&h)[2][3],
+                                          R (&nn)[3])
 {
     constexpr sn_stencil::Off o = sn_stencil::pair_offset(RC, TWO_D, I);
     constexpr int H = RC;
-    // signed byte offsets: neighbours below the target give negative deltas;
-    // tb + delta stays inside the tile because |o| <= halo.
-    const int ao = FX[H + o.x] + FY[H + o.y] + FZ[H + o.z];
-    const int bo = FX[H - o.x] + FY[H - o.y] + FZ[H - o.z];
-    const float *pa = reinterpret_cast<const float *>(base + ((int)tb + ao));
-    const float *pb = reinterpret_cast<const float *>(base + ((int)tb + bo));
+    // x, y: class-major axes, per-colour byte deltas FX, FY (one column base
+    // tb + FX + FY per (ox, oy), shared by the column's loads); z: plain
+    // axis, a compile-time delta of 12 bytes per site.  Signed arithmetic:
+    // neighbours below the target have negative deltas, and every neighbour
+    // lies inside the tile because |o| <= halo.
+    const int ao = FX[H + o.x] + FY[H + o.y];
+    const int bo = FX[H - o.x] + FY[H - o.y];
+    const float *pa = reinterpret_cast<const float *>(base + ((int)tb + ao) + 12 * o.z);
+    const float *pb = reinterpret_cast<const float *>(base + ((int)tb + bo) - 12 * o.z);
     const R ax = pa[0], ay = pa[1], az = pa[2];
     const R bx = pb[0], by = pb[1], bz = pb[2];
     const R qx = ax + bx, qy = ay + by, qz = az + bz;
@@ -89,7 +101,7 @@ __device__ __forceinline__ void pair_step(const unsigned char *__restrict__ base
     if constexpr (o.x * o.x + o.y * o.y + o.z * o.z == 1) {
         if constexpr (MIXED) {
             // the tile holds len*p; the cage-strain term wants unit p
-            const R la = tlen[(int)tslot + ao / 12], lb = tlen[(int)tslot + bo / 12];
+            const R la = tlen[(int)tslot + ao / 12 + o.z], lb = tlen[(int)tslot + bo / 12 - o.z];
             const R ia = la > R(0) ? R(1) / la : R(0), ib = lb > R(0) ? R(1) / lb : R(0);
             nn[0] += ax * ia + bx * ib;
             nn[1] += ay * ia + by * ib;
@@ -105,26 +117,24 @@ __device__ __forceinline__ void pair_step(const unsigned char *__restrict__ base
 template <typename R, int RC, bool TWO_D, bool MIXED, int LO, int... Is>
 __device__ __forceinline__ void run_pairs(std::integer_sequence<int, Is...>, const unsigned char *base, uint32_t tb,
                                           const int (&FX)[2 * RC + 1], const int (&FY)[2 * RC + 1],
-                                          const int (&FZ)[2 * RC + 1], const float *tlen, uint32_t tslot,
-                                          R (&h)[2][3], R (&nn)[3])
+                                          const float *tlen, uint32_t tslot, R (&h)[2][3], R (&nn)[3])
 {
-    (pair_step<R, RC, TWO_D, MIXED, LO + Is>(base, tb, FX, FY, FZ, tlen, tslot, h, nn), ...);
+    (pair_step<R, RC, TWO_D, MIXED, LO + Is>(base, tb, FX, FY, tlen, tslot, h, nn), ...);
 }
 
 template <typename R, int RC, bool TWO_D, bool MIXED, int J>
 __device__ __forceinline__ void dispatch_split(int j, const unsigned char *base, uint32_t tb,
                                                const int (&FX)[2 * RC + 1], const int (&FY)[2 * RC + 1],
-                                               const int (&FZ)[2 * RC + 1], const float *tlen, uint32_t tslot,
-                                               R (&h)[2][3], R (&nn)[3])
+                                               const float *tlen, uint32_t tslot, R (&h)[2][3], R (&nn)[3])
 {
     using G = Geo<RC, TWO_D>;
     if constexpr (J < G::NS) {
         if (j == J) {
             constexpr int lo = J * G::NP / G::NS, hi = (J + 1) * G::NP / G::NS;
-            run_pairs<R, RC, TWO_D, MIXED, lo>(std::make_integer_sequence<int, hi - lo>{}, base, tb, FX, FY, FZ,
-                                                tlen, tslot, h, nn);
+            run_pairs<R, RC, TWO_D, MIXED, lo>(std::make_integer_sequence<int, hi - lo>{}, base, tb, FX, FY, tlen,
+                                                tslot, h, nn);
         } else {
-            dispatch_split<R, RC, TWO_D, MIXED, J + 1>(j, base, tb, FX, FY, FZ, tlen, tslot, h, nn);
+            dispatch_split<R, RC, TWO_D, MIXED, J + 1>(j, base, tb, FX, FY, tlen, tslot, h, nn);
         }
     }
 }
@@ -134,7 +144,7 @@ __device__ __forceinline__ int sn_wrap(int v, int L) { return v < 0 ? v + L : (v
 template <int S>
 __device__ __forceinline__ int sn_pi(const int *start, int u) { return start[u % S] + u / S; }
 
-__device__ __forceinline__ int sn_count(int B, int c, int S) { return c < B ? (B - c + S - 1) / S : 0; }
+__host__ __device__ inline int sn_count(int B, int c, int S) { return c < B ? (B - c + S - 1) / S : 0; }
 
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -143,14 +153,42 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// Compensated (Kahan) FP32 running sum: error independent of the number of
+// terms to first order, so a thread's few dozen accepted moves per block
+// keep FP64-grade totals without using the (slow) FP64 pipe per move.
+struct KahanF {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float v)
+    {
+        const float y = __fsub_rn(v, c);
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ void cp_async4(void *smem_dst, const void *gsrc)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Shared-memory carve-up, identical on host (sizing) and device.
 struct Carve {
-    uint32_t tile, tlen, props, psite, parts, ftab, start, red, total;
+    uint32_t tile, tlen, props, parts, ftab, start, red, total;
 };
 
 __host__ __device__ inline uint32_t sn_align16(uint32_t v) { return (v + 15u) & ~15u; }
 
-__host__ __device__ inline Carve sn_carve(int slots, int maxt, int S, int SZ, int NS, int NF, bool mixed)
+// pc > 0: sweep kernel (pc staged proposal groups, 3 float partials);
+// pc == 0: field kernel (6 partials of rbytes each).
+__host__ __device__ inline Carve sn_carve(int slots, int tg, int pc, int NS, int S, int NF, bool mixed, int rbytes)
 {
     Carve c;
     uint32_t o = 0;
@@ -159,241 +197,286 @@ __host__ __device__ inline Carve sn_carve(int slots, int maxt, int S, int SZ, in
     c.tlen = o;
     if (mixed) o += sn_align16((uint32_t)slots * 4u);
     c.props = o;
-    o += (uint32_t)(S * SZ * maxt) * 16u;
-    c.psite = o;
-    o += sn_align16((uint32_t)(S * SZ * maxt) * 4u);
+    o += (uint32_t)(pc * tg) * 16u;
     c.parts = o;
-    o += sn_align16((uint32_t)(NS * 6 * maxt) * 8u);  // room for FP64 partials (field kernel)
+    o += sn_align16((uint32_t)(NS * (pc > 0 ? 3 : 6) * tg * rbytes));
     c.ftab = o;
     o += sn_align16((uint32_t)(3 * S * NF) * 4u);
     c.start = o;
     o += sn_align16(3u * SN_MAX_S * 4u);
     c.red = o;
-    o += (SN_THREADS / 32) * 16u * 8u;
+    o += (SN_MAX_THREADS / 32) * 16u * 8u;
     c.total = o;
     return c;
 }
 
-// ---------------------------------------------------------------------------
+// Colour (cx, cy, cz) of half `h` of group g (h = 1: the merged partner).
+template <int S, int SZ, bool MERGE>
+__device__ __forceinline__ void group_colour(int g, int h, int &cx, int &cy, int &cz)
+{
+    cx = g / (S * SZ);
+    cy = (g / SZ) % S;
+    cz = g % SZ;
+    if (MERGE && h) {
+        cx = (cx + S / 2) % S;
+        cy = (cy + S / 2) % S;
+        cz = (cz + S / 2) % S;
+    }
+}
+
+// Tables every block needs: class starts of the x and y axes and, per axis
+// and site colour c, the byte delta of each offset o from a target of
+// colour c (z is stored plainly: its deltas are compile-time).
+template <int RC, bool TWO_D>
+__device__ __forceinline__ void build_tables(const SnTile &Gm, int *start, int *ftab, int tid, int nthreads)
+{
+    using G = Geo<RC, TWO_D>;
+    constexpr int S = G::S, H = G::H, NF = G::NF;
+    if (tid < 3 * SN_MAX_S) start[tid] = Gm.start[tid / SN_MAX_S][tid % SN_MAX_S];
+    __syncthreads();
+    for (int i = tid; i < 2 * S * NF; i += nthreads) {
+        const int ax = i / (S * NF), c = (i / NF) % S, o = i % NF - H;
+        int v = 0;
+        const int T = Gm.T[ax];
+        const int u0 = c + H, u = u0 + o;
+        if (u >= 0 && u < T && u0 < T) {
+            const int *st = start + ax * SN_MAX_S;
+            const int d = sn_pi<S>(st, u) - sn_pi<S>(st, u0);
+            v = d * (ax == 0 ? Gm.Sx : Gm.Sy) * 12;
+        }
+        ftab[i] = v;
+    }
+}
+
+// Asynchronous copy of block + halo (periodic wrap) into the class-major tile.
 template <int RC, bool TWO_D, bool MIXED>
-__global__ void __launch_bounds__(SN_THREADS, 1) sweep_phase(const SnPhaseArgs a)
+__device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, float *tile,
+                                           float *tlen, const int *start, int tid, int nthreads)
+{
+    using G = Geo<RC, TWO_D>;
+    constexpr int S = G::S, H = G::H, HZ = G::HZ;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nthreads >> 5;
+    const int X = R.X, Y = R.Y, Z = R.Z;
+    const int Tx = Gm.T[0], Ty = Gm.T[1], Tz = Gm.T[2];
+    for (int row = warp; row < Tx * Ty; row += nwarps) {
+        const int ux = row / Ty, uy = row - (row / Ty) * Ty;
+        const int gx = sn_wrap(w.x0 - H + ux, X), gy = sn_wrap(w.y0 - H + uy, Y);
+        const int rslot = sn_pi<S>(start, ux) * Gm.Sx + sn_pi<S>(start + SN_MAX_S, uy) * Gm.Sy;
+        const long long gb = ((long long)gx * Y + gy) * Z;
+        for (int uz = lane; uz < Tz; uz += 32) {
+            const int gz = TWO_D ? 0 : sn_wrap(w.z0 - HZ + uz, Z);
+            const long long g = gb + gz;
+            const int slot = rslot + uz;  // z is stored plainly
+            cp_async4(&tile[3 * slot + 0], R.px + g);
+            cp_async4(&tile[3 * slot + 1], R.py + g);
+            cp_async4(&tile[3 * slot + 2], R.pz + g);
+            if constexpr (MIXED) cp_async4(&tlen[slot], R.len + g);
+        }
+    }
+}
+
+// The tile of a mixed-length lattice holds len * p.
+template <bool MIXED>
+__device__ __forceinline__ void scale_tile(float *tile, const float *tlen, int slots, int tid, int nthreads)
+{
+    if constexpr (MIXED) {
+        for (int i = tid; i < slots; i += nthreads) {
+            const float L = tlen[i];
+            tile[3 * i + 0] *= L;
+            tile[3 * i + 1] *= L;
+            tile[3 * i + 2] *= L;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sweep kernel.  Thread tid owns split j = tid / tg of the stencil for target
+// tt = tid % tg of every colour group: half h = tt / tp of the group, target
+// t = tt % tp = (qx, qy, qz) of that colour (inactive where the colour has
+// fewer targets).  Threads with j == 0 also finalize their target.
+template <int RC, bool TWO_D, bool MIXED>
+__global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseArgs a)
 {
     using G = Geo<RC, TWO_D>;
     constexpr int S = G::S, H = G::H, HZ = G::HZ, SZ = G::SZ, NF = G::NF, NS = G::NS;
+    constexpr bool MERGE = G::MERGE;
     extern __shared__ __align__(16) unsigned char smem[];
 
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, nthreads = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5;
     const SnWork w = a.work[blockIdx.x];
     const SnReplicaDev &R = a.reps[w.rep];
     const SnTile &Gm = a.geoms[R.geom];
 
-    const int X = R.X, Y = R.Y, Z = R.Z;
+    const int Y = R.Y, Z = R.Z;
     float *__restrict__ gpx = R.px;
     float *__restrict__ gpy = R.py;
     float *__restrict__ gpz = R.pz;
     const float *__restrict__ glen = R.len;
     const int Bx = Gm.B[0], By = Gm.B[1], Bz = Gm.B[2];
-    const int Tx = Gm.T[0], Ty = Gm.T[1], Tz = Gm.T[2];
-    const int Sy = Gm.Sy, Sx = Gm.Sx, maxt = Gm.maxt;
+    const int Sy = Gm.Sy, Sx = Gm.Sx;
+    const int tp = Gm.tp, tg = Gm.tg, ng = Gm.ng, pc = Gm.pc;
+    const int nqy = Gm.nq[1], nqz = Gm.nq[2];
     const uint32_t sweep = *a.sweep;
     const uint2 key = make_uint2(R.seed_lo, R.seed_hi);
     const float beta = R.beta;
     const float Ex = R.E[0], Ey = R.E[1], Ez = R.E[2];
     const float C = a.cage, Kk = a.K;
     const float Lu = R.length;
-    const float gscale = MIXED ? 1.0f : Lu * Lu;
 
-    const Carve cv = sn_carve(Gm.slots, maxt, S, SZ, NS, NF, MIXED);
+    const Carve cv = sn_carve(Gm.slots, tg, pc, NS, S, NF, MIXED, 4);
     float *tile = reinterpret_cast<float *>(smem + cv.tile);
     float *tlen = reinterpret_cast<float *>(smem + cv.tlen);
     float4 *props = reinterpret_cast<float4 *>(smem + cv.props);
-    int *psite = reinterpret_cast<int *>(smem + cv.psite);
     float *parts = reinterpret_cast<float *>(smem + cv.parts);
     int *ftab = reinterpret_cast<int *>(smem + cv.ftab);
     int *start = reinterpret_cast<int *>(smem + cv.start);
     double *red = reinterpret_cast<double *>(smem + cv.red);
 
-    // ---- geometry tables ---------------------------------------------------
-    if (tid < 3 * SN_MAX_S) start[tid] = Gm.start[tid / SN_MAX_S][tid % SN_MAX_S];
-    __syncthreads();
-    for (int i = tid; i < 3 * S * NF; i += SN_THREADS) {
-        const int ax = i / (S * NF), c = (i / NF) % S, o = i % NF - H;
-        int v = 0;
-        const int Ha = ax == 2 ? HZ : H;
-        const int T = Gm.T[ax];
-        const int u0 = c + Ha, u = u0 + o;
-        if (!(ax == 2 && TWO_D) && u >= 0 && u < T && u0 < T) {
-            const int *st = start + ax * SN_MAX_S;
-            const int d = sn_pi<S>(st, u) - sn_pi<S>(st, u0);
-            const int stride = ax == 0 ? Sx : (ax == 1 ? Sy : 1);
-            v = d * stride * 12;
-        }
-        ftab[i] = v;
-    }
+    build_tables<RC, TWO_D>(Gm, start, ftab, tid, nthreads);
+    stage_tile<RC, TWO_D, MIXED>(R, Gm, w, tile, tlen, start, tid, nthreads);
 
-    // ---- stage block + halo (periodic wrap) ------------------------------------
-    for (int row = warp; row < Tx * Ty; row += SN_THREADS / 32) {
-        const int ux = row / Ty, uy = row - (row / Ty) * Ty;
-        const int gx = sn_wrap(w.x0 - H + ux, X), gy = sn_wrap(w.y0 - H + uy, Y);
-        const int rslot = sn_pi<S>(start, ux) * Sx + sn_pi<S>(start + SN_MAX_S, uy) * Sy;
-        const long long gb = ((long long)gx * Y + gy) * Z;
-        for (int uz = lane; uz < Tz; uz += 32) {
-            const int gz = TWO_D ? 0 : sn_wrap(w.z0 - HZ + uz, Z);
-            const long long g = gb + gz;
-            const int slot = rslot + (TWO_D ? 0 : sn_pi<S>(start + 2 * SN_MAX_S, uz));
-            float x = gpx[g], y = gpy[g], z = gpz[g];
-            if constexpr (MIXED) {
-                const float L = glen[g];
-                tlen[slot] = L;
-                x *= L;
-                y *= L;
-                z *= L;
-            }
-            tile[3 * slot + 0] = x;
-            tile[3 * slot + 1] = y;
-            tile[3 * slot + 2] = z;
-        }
-    }
-    __syncthreads();
+    // this thread's fixed role
+    const int j = tid / tg, tt = tid - (tid / tg) * tg;
+    const int hh = tt / tp, t = tt - (tt / tp) * tp;
+    const int qz = t % nqz, qy = (t / nqz) % nqy, qx = t / (nqz * nqy);
+    // a launch shared by replicas of different geometry runs with the largest
+    // block size: threads past splits * targets have no stencil role
+    const bool tvalid = tid < NS * tg && qx < Gm.nq[0];
+    const int trel = qx * Sx + qy * Sy + S * qz;  // z plain: targets S apart
+    const int srel = ((S * qx) * Y + S * qy) * Z + (TWO_D ? 0 : S * qz);
 
-    double sdE = 0.0, sPx = 0.0, sPy = 0.0, sPz = 0.0;
+    KahanF sdE, sPx, sPy, sPz;
     unsigned int sacc = 0, satt = 0;
 
-    for (int cx = 0; cx < S; cx++) {
-        const int nxc = sn_count(Bx, cx, S);
-        if (nxc == 0) continue;
-        // ---- proposals for every (cy, cz) of this cx: independent of the lattice
-        for (int i = tid; i < S * SZ * maxt; i += SN_THREADS) {
-            const int k = i / maxt, t = i - k * maxt;
-            const int cy = k / SZ, cz = k - cy * SZ;
-            const int nyc = sn_count(By, cy, S), nzc = TWO_D ? 1 : sn_count(Bz, cz, S);
-            if (t >= nxc * nyc * nzc) continue;
-            const int qz = t % nzc, r = t / nzc, qy = r % nyc, qx = r / nyc;
-            const int lx = cx + S * qx, ly = cy + S * qy, lz = TWO_D ? 0 : cz + S * qz;
-            const int site = ((w.x0 + lx) * Y + (w.y0 + ly)) * Z + (w.z0 + lz);
-            const int slot = sn_pi<S>(start, lx + H) * Sx + sn_pi<S>(start + SN_MAX_S, ly + H) * Sy +
-                             (TWO_D ? 0 : sn_pi<S>(start + 2 * SN_MAX_S, lz + HZ));
-            bool occ;
-            if constexpr (MIXED) occ = tlen[slot] != 0.0f;
-            else occ = tile[3 * slot] != 0.0f || tile[3 * slot + 1] != 0.0f || tile[3 * slot + 2] != 0.0f;
-            float4 pr = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-            if (occ) {
-                float3 p;
-                float u;
-                if (!sn_proposal((uint32_t)site, sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
-                    p = make_float3(gpx[site], gpy[site], gpz[site]);
-                pr = make_float4(p.x, p.y, p.z, u);
+    int FX[NF], FY[NF];
+    int pcx = -1, pcy = -1;
+    int gchunk = 0, gnext = 0;  // first group of the staged chunk, first group of the next
+    // groups in which this thread's target exists (bit g), computed once
+    unsigned long long amask = 0ull;
+    for (int g = 0; g < ng && g < 64; g++) {
+        int cx, cy, cz;
+        group_colour<S, SZ, MERGE>(g, hh, cx, cy, cz);
+        if (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) && (TWO_D || qz < sn_count(Bz, cz, S)))
+            amask |= 1ull << g;
+    }
+    for (int g = 0; g < ng; g++) {
+        // ---- proposals and accept thresholds of the next pc groups ------------
+        // Thread (j, tt) draws for its own target tt in groups g0+j, g0+j+NS, ...
+        if (g == gnext) {
+            __syncthreads();  // previous chunk fully consumed
+            gchunk = g;
+            gnext = min(g + pc, ng);
+            if (tid < NS * tg) {
+                for (int k = j; k < gnext - g; k += NS) {
+                    int cx, cy, cz;
+                    group_colour<S, SZ, MERGE>(g + k, hh, cx, cy, cz);
+                    float4 pr = make_float4(0.0f, 0.0f, 0.0f, -2.0f);  // no target here
+                    if ((g + k < 64) ? ((amask >> (g + k)) & 1ull)
+                                     : (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
+                                        (TWO_D || qz < sn_count(Bz, cz, S)))) {
+                        const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + (TWO_D ? 0 : w.z0 + cz) + srel;
+                        pr.w = -1.0f;  // vacancy
+                        if (glen[site] != 0.0f) {
+                            float3 p;
+                            float u;
+                            if (!sn_proposal((uint32_t)site, sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
+                                p = make_float3(gpx[site], gpy[site], gpz[site]);
+                            // accept iff dE < -ln(u)/beta  <=>  dE < 0 || exp(-beta dE) > u
+                            const float thr = u > 0.0f ? -logf(u) / beta : INFINITY;
+                            pr = make_float4(p.x, p.y, p.z, thr);
+                        }
+                    }
+                    props[k * tg + tt] = pr;
+                }
             }
-            props[i] = pr;
-            psite[i] = site;
+            if (g == 0) cp_async_wait_all();
+            __syncthreads();
+            if (g == 0) scale_tile<MIXED>(tile, tlen, Gm.slots, tid, nthreads);
         }
-        __syncthreads();
-        int FX[NF];
-#pragma unroll
-        for (int o = 0; o < NF; o++) FX[o] = ftab[(0 * S + cx) * NF + o];
-        const int bx0 = sn_pi<S>(start, cx + H);
 
-        for (int cy = 0; cy < S; cy++) {
-            const int nyc = sn_count(By, cy, S);
-            if (nyc == 0) continue;
-            int FY[NF];
+        int cx, cy, cz;
+        group_colour<S, SZ, MERGE>(g, hh, cx, cy, cz);
+        const bool active = (g < 64) ? ((amask >> g) & 1ull) != 0ull
+                                     : (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
+                                        (TWO_D || qz < sn_count(Bz, cz, S)));
+        if (cx != pcx) {
+#pragma unroll
+            for (int o = 0; o < NF; o++) FX[o] = ftab[(0 * S + cx) * NF + o];
+            pcx = cx;
+        }
+        if (cy != pcy) {
 #pragma unroll
             for (int o = 0; o < NF; o++) FY[o] = ftab[(1 * S + cy) * NF + o];
-            const int by0 = sn_pi<S>(start + SN_MAX_S, cy + H);
+            pcy = cy;
+        }
+        const int tslot = sn_pi<S>(start, cx + H) * Sx + sn_pi<S>(start + SN_MAX_S, cy + H) * Sy +
+                          (TWO_D ? 0 : cz + HZ) + trel;
 
-            for (int cz = 0; cz < SZ; cz++) {
-                const int nzc = TWO_D ? 1 : sn_count(Bz, cz, S);
-                const int nt = nxc * nyc * nzc;
-                if (nt == 0) continue;
-                int FZ[NF];
+        // ---- 1. partial g = len_i h - C nn of this split ---------------------------
+        if (active) {
+            float hacc[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+            float nn[3] = {0.f, 0.f, 0.f};
+            dispatch_split<float, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, (uint32_t)tslot * 12u, FX, FY, tlen,
+                                                       (uint32_t)tslot, hacc, nn);
+            const float sc = MIXED ? tlen[tslot] : Lu * Lu;
+            float *pp = parts + (j * 3) * tg + tt;
+            pp[0 * tg] = fmaf(sc, hacc[0][0] + hacc[1][0], -C * nn[0]);
+            pp[1 * tg] = fmaf(sc, hacc[0][1] + hacc[1][1], -C * nn[1]);
+            pp[2 * tg] = fmaf(sc, hacc[0][2] + hacc[1][2], -C * nn[2]);
+        }
+        __syncthreads();
+
+        // ---- 2. finalize: dE, accept, update ------------------------------------------
+        if (j == 0 && active) {
+            const float4 pr = props[(g - gchunk) * tg + tt];
+            if (pr.w >= 0.0f) {
+                float gx = Ex, gy = Ey, gz = Ez;
 #pragma unroll
-                for (int o = 0; o < NF; o++) FZ[o] = TWO_D ? 0 : ftab[(2 * S + cz) * NF + o];
-                const int bz0 = TWO_D ? 0 : sn_pi<S>(start + 2 * SN_MAX_S, cz + HZ);
-                const int ntp = (nt + 31) & ~31;
-
-                // ---- 1. partial local fields ----------------------------------
-                for (int wi = tid; wi < NS * ntp; wi += SN_THREADS) {
-                    const int j = wi / ntp, t = wi - j * ntp;
-                    if (t < nt) {
-                        const int qz = t % nzc, r = t / nzc, qy = r % nyc, qx = r / nyc;
-                        const uint32_t tslot = (uint32_t)((bx0 + qx) * Sx + (by0 + qy) * Sy + bz0 + qz);
-                        float hacc[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-                        float nn[3] = {0.f, 0.f, 0.f};
-                        dispatch_split<float, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, tslot * 12u, FX, FY, FZ, tlen, tslot,
-                                                            hacc, nn);
-                        float *pp = parts + (j * 6) * maxt + t;
-                        pp[0 * maxt] = hacc[0][0] + hacc[1][0];
-                        pp[1 * maxt] = hacc[0][1] + hacc[1][1];
-                        pp[2 * maxt] = hacc[0][2] + hacc[1][2];
-                        pp[3 * maxt] = nn[0];
-                        pp[4 * maxt] = nn[1];
-                        pp[5 * maxt] = nn[2];
-                    }
+                for (int k = 0; k < NS; k++) {
+                    const float *pp = parts + (k * 3) * tg + tt;
+                    gx += pp[0 * tg];
+                    gy += pp[1 * tg];
+                    gz += pp[2 * tg];
                 }
-                __syncthreads();
-
-                // ---- 2. finalize: dE, accept, update --------------------------
-                for (int t = tid; t < nt; t += SN_THREADS) {
-                    const int pk = (cy * SZ + cz) * maxt + t;
-                    const float4 pr = props[pk];
-                    if (pr.w < 0.0f) continue;  // vacancy
-                    float hx = 0.f, hy = 0.f, hz = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
-#pragma unroll
-                    for (int j = 0; j < NS; j++) {
-                        const float *pp = parts + (j * 6) * maxt + t;
-                        hx += pp[0 * maxt];
-                        hy += pp[1 * maxt];
-                        hz += pp[2 * maxt];
-                        nx += pp[3 * maxt];
-                        ny += pp[4 * maxt];
-                        nz += pp[5 * maxt];
-                    }
-                    const int qz = t % nzc, r = t / nzc, qy = r % nyc, qx = r / nyc;
-                    const int tslot = (bx0 + qx) * Sx + (by0 + qy) * Sy + bz0 + qz;
-                    const int site = psite[pk];
-                    float Li, ox, oy, oz;
-                    if constexpr (MIXED) {
-                        Li = tlen[tslot];
-                        ox = gpx[site];
-                        oy = gpy[site];
-                        oz = gpz[site];
-                    } else {
-                        Li = Lu;
-                        ox = tile[3 * tslot + 0];
-                        oy = tile[3 * tslot + 1];
-                        oz = tile[3 * tslot + 2];
-                    }
-                    const float sc = MIXED ? Li : gscale;
-                    const float gx = fmaf(sc, hx, fmaf(-C, nx, Ex));
-                    const float gy = fmaf(sc, hy, fmaf(-C, ny, Ey));
-                    const float gz = fmaf(sc, hz, fmaf(-C, nz, Ez));
-                    const float dx = pr.x - ox, dy = pr.y - oy, dz = pr.z - oz;
-                    float dE = fmaf(dx, gx, fmaf(dy, gy, dz * gz));
-                    if (Kk > 0.0f) dE -= Kk * ((fabsf(pr.x) - fabsf(ox)) + (fabsf(pr.y) - fabsf(oy)));
-                    satt++;
-                    const bool acc = (dE < 0.0f) || (expf(-beta * dE) > pr.w);
-                    if (acc) {
-                        tile[3 * tslot + 0] = MIXED ? Li * pr.x : pr.x;
-                        tile[3 * tslot + 1] = MIXED ? Li * pr.y : pr.y;
-                        tile[3 * tslot + 2] = MIXED ? Li * pr.z : pr.z;
-                        gpx[site] = pr.x;
-                        gpy[site] = pr.y;
-                        gpz[site] = pr.z;
-                        sacc++;
-                        sdE += (double)dE;
-                        sPx += (double)(Li * dx);
-                        sPy += (double)(Li * dy);
-                        sPz += (double)(Li * dz);
-                    }
+                const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + (TWO_D ? 0 : w.z0 + cz) + srel;
+                float Li, ox, oy, oz;
+                if constexpr (MIXED) {
+                    Li = tlen[tslot];
+                    ox = gpx[site];
+                    oy = gpy[site];
+                    oz = gpz[site];
+                } else {
+                    Li = Lu;
+                    ox = tile[3 * tslot + 0];
+                    oy = tile[3 * tslot + 1];
+                    oz = tile[3 * tslot + 2];
                 }
-                __syncthreads();
+                const float dx = pr.x - ox, dy = pr.y - oy, dz = pr.z - oz;
+                float dE = fmaf(dx, gx, fmaf(dy, gy, dz * gz));
+                if (Kk > 0.0f) dE -= Kk * ((fabsf(pr.x) - fabsf(ox)) + (fabsf(pr.y) - fabsf(oy)));
+                satt++;
+                if (dE < pr.w) {
+                    tile[3 * tslot + 0] = MIXED ? Li * pr.x : pr.x;
+                    tile[3 * tslot + 1] = MIXED ? Li * pr.y : pr.y;
+                    tile[3 * tslot + 2] = MIXED ? Li * pr.z : pr.z;
+                    gpx[site] = pr.x;
+                    gpy[site] = pr.y;
+                    gpz[site] = pr.z;
+                    sacc++;
+                    sdE.add(dE);
+                    sPx.add(Li * dx);
+                    sPy.add(Li * dy);
+                    sPz.add(Li * dz);
+                }
             }
         }
+        __syncthreads();
     }
 
     // ---- block reduction of the move statistics ---------------------------------
-    double v[6] = {sdE, sPx, sPy, sPz, (double)sacc, (double)satt};
+    double v[6] = {sdE.value(), sPx.value(), sPy.value(), sPz.value(), (double)sacc, (double)satt};
 #pragma unroll
     for (int k = 0; k < 6; k++) v[k] = warp_sum(v[k]);
     if (lane == 0) {
@@ -401,26 +484,22 @@ __global__ void __launch_bounds__(SN_THREADS, 1) sweep_phase(const SnPhaseArgs a
         for (int k = 0; k < 6; k++) red[warp * 16 + k] = v[k];
     }
     __syncthreads();
-    if (tid == 0) {
-        double t[6] = {0, 0, 0, 0, 0, 0};
-        for (int q = 0; q < SN_THREADS / 32; q++)
-            for (int k = 0; k < 6; k++) t[k] += red[q * 16 + k];
+    if (tid < 6) {
+        double s = 0.0;
+        for (int q = 0; q < (nthreads >> 5); q++) s += red[q * 16 + tid];
         SnAccum *A = a.acc + w.rep;
-        atomicAdd(&A->dE, t[0]);
-        atomicAdd(&A->dP[0], t[1]);
-        atomicAdd(&A->dP[1], t[2]);
-        atomicAdd(&A->dP[2], t[3]);
-        atomicAdd(&A->acc, (unsigned long long)t[4]);
-        atomicAdd(&A->att, (unsigned long long)t[5]);
+        if (tid == 0) atomicAdd(&A->dE, s);
+        else if (tid < 4) atomicAdd(&A->dP[tid - 1], s);
+        else if (tid == 4) atomicAdd(&A->acc, (unsigned long long)s);
+        else atomicAdd(&A->att, (unsigned long long)s);
     }
 }
 
-
 // ---------------------------------------------------------------------------
 // Full local-field pass (energy recompute, site energies, adjoint).  Same
-// tiles and stencil as the sweep, read-only, every block of the replica in
-// one launch.  R = float: FP32 local fields, FP64 site products and sums;
-// R = double: every operation in FP64.
+// tiles, stencil and thread roles as the sweep, read-only, every block of
+// the replica in one launch.  R = float: FP32 local fields, FP64 site
+// products and sums; R = double: every operation in FP64.
 //   red[rep*red_stride + k]: 0 E_dd = 1/2 sum len_i p_i.H_i   1 sum p_i.nn_i
 //                    2 sum p_i.E                       3 sum K term
 //                    4..6 sum len_i p_i                7..9 sum p_i
@@ -438,30 +517,32 @@ struct SnFieldArgs {
 };
 
 template <typename R, int RC, bool TWO_D, bool MIXED>
-__global__ void __launch_bounds__(SN_THREADS, 1) field_tiled(const SnFieldArgs a)
+__global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldArgs a)
 {
     using G = Geo<RC, TWO_D>;
     constexpr int S = G::S, H = G::H, HZ = G::HZ, SZ = G::SZ, NF = G::NF, NS = G::NS;
+    constexpr bool MERGE = G::MERGE;
     extern __shared__ __align__(16) unsigned char smem[];
 
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, nthreads = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5;
     const SnWork w = a.work[blockIdx.x];
     const SnReplicaDev &Rp = a.reps[w.rep];
     const SnTile &Gm = a.geoms[Rp.geom];
-    const int X = Rp.X, Y = Rp.Y, Z = Rp.Z;
+    const int Y = Rp.Y, Z = Rp.Z;
     const float *__restrict__ gpx = Rp.px;
     const float *__restrict__ gpy = Rp.py;
     const float *__restrict__ gpz = Rp.pz;
     const float *__restrict__ glen = Rp.len;
     const int Bx = Gm.B[0], By = Gm.B[1], Bz = Gm.B[2];
-    const int Tx = Gm.T[0], Ty = Gm.T[1], Tz = Gm.T[2];
-    const int Sy = Gm.Sy, Sx = Gm.Sx, maxt = Gm.maxt;
+    const int Sy = Gm.Sy, Sx = Gm.Sx;
+    const int tp = Gm.tp, tg = Gm.tg, ng = Gm.ng;
+    const int nqy = Gm.nq[1], nqz = Gm.nq[2];
     const double C = a.cage, Kk = a.K;
     const double Ex = Rp.E[0], Ey = Rp.E[1], Ez = Rp.E[2];
     const R Lu = (R)Rp.length;
 
-    const Carve cv = sn_carve(Gm.slots, maxt, S, SZ, NS, NF, MIXED);
+    const Carve cv = sn_carve(Gm.slots, tg, 0, NS, S, NF, MIXED, (int)sizeof(R));
     float *tile = reinterpret_cast<float *>(smem + cv.tile);
     float *tlen = reinterpret_cast<float *>(smem + cv.tlen);
     R *parts = reinterpret_cast<R *>(smem + cv.parts);
@@ -469,147 +550,107 @@ __global__ void __launch_bounds__(SN_THREADS, 1) field_tiled(const SnFieldArgs a
     int *start = reinterpret_cast<int *>(smem + cv.start);
     double *red = reinterpret_cast<double *>(smem + cv.red);
 
-    if (tid < 3 * SN_MAX_S) start[tid] = Gm.start[tid / SN_MAX_S][tid % SN_MAX_S];
+    build_tables<RC, TWO_D>(Gm, start, ftab, tid, nthreads);
+    stage_tile<RC, TWO_D, MIXED>(Rp, Gm, w, tile, tlen, start, tid, nthreads);
+    cp_async_wait_all();
     __syncthreads();
-    for (int i = tid; i < 3 * S * NF; i += SN_THREADS) {
-        const int ax = i / (S * NF), c = (i / NF) % S, o = i % NF - H;
-        int v = 0;
-        const int Ha = ax == 2 ? HZ : H;
-        const int T = Gm.T[ax];
-        const int u0 = c + Ha, u = u0 + o;
-        if (!(ax == 2 && TWO_D) && u >= 0 && u < T && u0 < T) {
-            const int *st = start + ax * SN_MAX_S;
-            const int d = sn_pi<S>(st, u) - sn_pi<S>(st, u0);
-            const int stride = ax == 0 ? Sx : (ax == 1 ? Sy : 1);
-            v = d * stride * 12;
-        }
-        ftab[i] = v;
-    }
-    for (int row = warp; row < Tx * Ty; row += SN_THREADS / 32) {
-        const int ux = row / Ty, uy = row - (row / Ty) * Ty;
-        const int gx = sn_wrap(w.x0 - H + ux, X), gy = sn_wrap(w.y0 - H + uy, Y);
-        const int rslot = sn_pi<S>(start, ux) * Sx + sn_pi<S>(start + SN_MAX_S, uy) * Sy;
-        const long long gb = ((long long)gx * Y + gy) * Z;
-        for (int uz = lane; uz < Tz; uz += 32) {
-            const int gz = TWO_D ? 0 : sn_wrap(w.z0 - HZ + uz, Z);
-            const long long g = gb + gz;
-            const int slot = rslot + (TWO_D ? 0 : sn_pi<S>(start + 2 * SN_MAX_S, uz));
-            float x = gpx[g], y = gpy[g], z = gpz[g];
-            if constexpr (MIXED) {
-                const float L = glen[g];
-                tlen[slot] = L;
-                x *= L;
-                y *= L;
-                z *= L;
-            }
-            tile[3 * slot + 0] = x;
-            tile[3 * slot + 1] = y;
-            tile[3 * slot + 2] = z;
-        }
-    }
-    __syncthreads();
+    scale_tile<MIXED>(tile, tlen, Gm.slots, tid, nthreads);
+
+    const int j = tid / tg, tt = tid - (tid / tg) * tg;
+    const int hh = tt / tp, t = tt - (tt / tp) * tp;
+    const int qz = t % nqz, qy = (t / nqz) % nqy, qx = t / (nqz * nqy);
+    const bool tvalid = tid < NS * tg && qx < Gm.nq[0];
+    const int trel = qx * Sx + qy * Sy + S * qz;  // z plain: targets S apart
+    const int srel = ((S * qx) * Y + S * qy) * Z + (TWO_D ? 0 : S * qz);
 
     double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int cx = 0; cx < S; cx++) {
-        const int nxc = sn_count(Bx, cx, S);
-        if (nxc == 0) continue;
-        int FX[NF];
+    int FX[NF], FY[NF];
+    int pcx = -1, pcy = -1;
+    for (int g = 0; g < ng; g++) {
+        int cx, cy, cz;
+        group_colour<S, SZ, MERGE>(g, hh, cx, cy, cz);
+        const bool active = tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
+                            (TWO_D || qz < sn_count(Bz, cz, S));
+        if (cx != pcx) {
 #pragma unroll
-        for (int o = 0; o < NF; o++) FX[o] = ftab[(0 * S + cx) * NF + o];
-        const int bx0 = sn_pi<S>(start, cx + H);
-        for (int cy = 0; cy < S; cy++) {
-            const int nyc = sn_count(By, cy, S);
-            if (nyc == 0) continue;
-            int FY[NF];
+            for (int o = 0; o < NF; o++) FX[o] = ftab[(0 * S + cx) * NF + o];
+            pcx = cx;
+        }
+        if (cy != pcy) {
 #pragma unroll
             for (int o = 0; o < NF; o++) FY[o] = ftab[(1 * S + cy) * NF + o];
-            const int by0 = sn_pi<S>(start + SN_MAX_S, cy + H);
-            for (int cz = 0; cz < SZ; cz++) {
-                const int nzc = TWO_D ? 1 : sn_count(Bz, cz, S);
-                const int nt = nxc * nyc * nzc;
-                if (nt == 0) continue;
-                int FZ[NF];
+            pcy = cy;
+        }
+        const int tslot = sn_pi<S>(start, cx + H) * Sx + sn_pi<S>(start + SN_MAX_S, cy + H) * Sy +
+                          (TWO_D ? 0 : cz + HZ) + trel;
+        if (active) {
+            R hacc[2][3] = {{0, 0, 0}, {0, 0, 0}};
+            R nn[3] = {0, 0, 0};
+            dispatch_split<R, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, (uint32_t)tslot * 12u, FX, FY, tlen,
+                                                   (uint32_t)tslot, hacc, nn);
+            R *pp = parts + (j * 6) * tg + tt;
+            pp[0 * tg] = hacc[0][0] + hacc[1][0];
+            pp[1 * tg] = hacc[0][1] + hacc[1][1];
+            pp[2 * tg] = hacc[0][2] + hacc[1][2];
+            pp[3 * tg] = nn[0];
+            pp[4 * tg] = nn[1];
+            pp[5 * tg] = nn[2];
+        }
+        __syncthreads();
+        if (j == 0 && active) {
+            R hx = 0, hy = 0, hz = 0, nx = 0, ny = 0, nz = 0;
 #pragma unroll
-                for (int o = 0; o < NF; o++) FZ[o] = TWO_D ? 0 : ftab[(2 * S + cz) * NF + o];
-                const int bz0 = TWO_D ? 0 : sn_pi<S>(start + 2 * SN_MAX_S, cz + HZ);
-                const int ntp = (nt + 31) & ~31;
-                for (int wi = tid; wi < NS * ntp; wi += SN_THREADS) {
-                    const int j = wi / ntp, t = wi - j * ntp;
-                    if (t < nt) {
-                        const int qz = t % nzc, r = t / nzc, qy = r % nyc, qx = r / nyc;
-                        const uint32_t tslot = (uint32_t)((bx0 + qx) * Sx + (by0 + qy) * Sy + bz0 + qz);
-                        R hacc[2][3] = {{0, 0, 0}, {0, 0, 0}};
-                        R nn[3] = {0, 0, 0};
-                        dispatch_split<R, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, tslot * 12u, FX, FY, FZ, tlen, tslot,
-                                                               hacc, nn);
-                        R *pp = parts + (j * 6) * maxt + t;
-                        pp[0 * maxt] = hacc[0][0] + hacc[1][0];
-                        pp[1 * maxt] = hacc[0][1] + hacc[1][1];
-                        pp[2 * maxt] = hacc[0][2] + hacc[1][2];
-                        pp[3 * maxt] = nn[0];
-                        pp[4 * maxt] = nn[1];
-                        pp[5 * maxt] = nn[2];
-                    }
+            for (int k = 0; k < NS; k++) {
+                const R *pp = parts + (k * 6) * tg + tt;
+                hx += pp[0 * tg];
+                hy += pp[1 * tg];
+                hz += pp[2 * tg];
+                nx += pp[3 * tg];
+                ny += pp[4 * tg];
+                nz += pp[5 * tg];
+            }
+            const long long site = ((long long)(w.x0 + cx) * Y + (w.y0 + cy)) * Z + (TWO_D ? 0 : w.z0 + cz) + srel;
+            const double px = gpx[site], py = gpy[site], pz = gpz[site];
+            const double Li = MIXED ? (double)glen[site] : (double)Rp.length;
+            if (Li == 0.0) {
+                if (a.site_e) a.site_e[site] = 0.0;
+                if (a.grad) {
+                    a.grad[3 * site + 0] = 0.0f;
+                    a.grad[3 * site + 1] = 0.0f;
+                    a.grad[3 * site + 2] = 0.0f;
                 }
-                __syncthreads();
-                for (int t = tid; t < nt; t += SN_THREADS) {
-                    R hx = 0, hy = 0, hz = 0, nx = 0, ny = 0, nz = 0;
-#pragma unroll
-                    for (int j = 0; j < NS; j++) {
-                        const R *pp = parts + (j * 6) * maxt + t;
-                        hx += pp[0 * maxt];
-                        hy += pp[1 * maxt];
-                        hz += pp[2 * maxt];
-                        nx += pp[3 * maxt];
-                        ny += pp[4 * maxt];
-                        nz += pp[5 * maxt];
-                    }
-                    const int qz = t % nzc, r = t / nzc, qy = r % nyc, qx = r / nyc;
-                    const int lx = cx + S * qx, ly = cy + S * qy, lz = TWO_D ? 0 : cz + S * qz;
-                    const long long site = ((long long)(w.x0 + lx) * Y + (w.y0 + ly)) * Z + (w.z0 + lz);
-                    const double px = gpx[site], py = gpy[site], pz = gpz[site];
-                    const double Li = MIXED ? (double)glen[site] : (double)Rp.length;
-                    if (Li == 0.0) {
-                        if (a.site_e) a.site_e[site] = 0.0;
-                        if (a.grad) {
-                            a.grad[3 * site + 0] = 0.0f;
-                            a.grad[3 * site + 1] = 0.0f;
-                            a.grad[3 * site + 2] = 0.0f;
-                        }
-                        continue;
-                    }
-                    // H = sum_j len_j T p_j: uniform tiles hold unit p (H = L h)
-                    const R sc = MIXED ? R(1) : Lu;
-                    const double Hx = (double)(sc * hx), Hy = (double)(sc * hy), Hz = (double)(sc * hz);
-                    const double gx = Li * Hx - C * (double)nx + Ex;
-                    const double gy = Li * Hy - C * (double)ny + Ey;
-                    const double gz = Li * Hz - C * (double)nz + Ez;
-                    const double kt = Kk > 0.0 ? -Kk * (fabs(px) + fabs(py)) : 0.0;
-                    const double pH = px * Hx + py * Hy + pz * Hz;
-                    const double pn = px * (double)nx + py * (double)ny + pz * (double)nz;
-                    const double pE = px * Ex + py * Ey + pz * Ez;
-                    if (a.site_e) a.site_e[site] = px * gx + py * gy + pz * gz + kt;
-                    if (a.grad) {
-                        const double sx = Kk > 0.0 ? (px > 0.0 ? 1.0 : (px < 0.0 ? -1.0 : 0.0)) : 0.0;
-                        const double sy = Kk > 0.0 ? (py > 0.0 ? 1.0 : (py < 0.0 ? -1.0 : 0.0)) : 0.0;
-                        a.grad[3 * site + 0] = (float)(gx - Kk * sx);
-                        a.grad[3 * site + 1] = (float)(gy - Kk * sy);
-                        a.grad[3 * site + 2] = (float)gz;
-                    }
-                    acc[0] += 0.5 * Li * pH;
-                    acc[1] += pn;
-                    acc[2] += pE;
-                    acc[3] += kt;
-                    acc[4] += Li * px;
-                    acc[5] += Li * py;
-                    acc[6] += Li * pz;
-                    acc[7] += px;
-                    acc[8] += py;
-                    acc[9] += pz;
+            } else {
+                // H = sum_j len_j T p_j: uniform tiles hold unit p (H = L h)
+                const R sc = MIXED ? R(1) : Lu;
+                const double Hx = (double)(sc * hx), Hy = (double)(sc * hy), Hz = (double)(sc * hz);
+                const double gx = Li * Hx - C * (double)nx + Ex;
+                const double gy = Li * Hy - C * (double)ny + Ey;
+                const double gz = Li * Hz - C * (double)nz + Ez;
+                const double kt = Kk > 0.0 ? -Kk * (fabs(px) + fabs(py)) : 0.0;
+                const double pH = px * Hx + py * Hy + pz * Hz;
+                const double pn = px * (double)nx + py * (double)ny + pz * (double)nz;
+                const double pE = px * Ex + py * Ey + pz * Ez;
+                if (a.site_e) a.site_e[site] = px * gx + py * gy + pz * gz + kt;
+                if (a.grad) {
+                    const double sx = Kk > 0.0 ? (px > 0.0 ? 1.0 : (px < 0.0 ? -1.0 : 0.0)) : 0.0;
+                    const double sy = Kk > 0.0 ? (py > 0.0 ? 1.0 : (py < 0.0 ? -1.0 : 0.0)) : 0.0;
+                    a.grad[3 * site + 0] = (float)(gx - Kk * sx);
+                    a.grad[3 * site + 1] = (float)(gy - Kk * sy);
+                    a.grad[3 * site + 2] = (float)gz;
                 }
-                __syncthreads();
+                acc[0] += 0.5 * Li * pH;
+                acc[1] += pn;
+                acc[2] += pE;
+                acc[3] += kt;
+                acc[4] += Li * px;
+                acc[5] += Li * py;
+                acc[6] += Li * pz;
+                acc[7] += px;
+                acc[8] += py;
+                acc[9] += pz;
             }
         }
+        __syncthreads();
     }
 #pragma unroll
     for (int k = 0; k < 10; k++) acc[k] = warp_sum(acc[k]);
@@ -619,14 +660,14 @@ __global__ void __launch_bounds__(SN_THREADS, 1) field_tiled(const SnFieldArgs a
     }
     __syncthreads();
     if (tid < 10) {
-        double t = 0.0;
-        for (int q = 0; q < SN_THREADS / 32; q++) t += red[q * 16 + tid];
-        atomicAdd(&a.red[a.red_stride * w.rep + tid], t);
+        double s = 0.0;
+        for (int q = 0; q < (nthreads >> 5); q++) s += red[q * 16 + tid];
+        atomicAdd(&a.red[a.red_stride * w.rep + tid], s);
     }
 }
 
 template <typename R, int RC>
-cudaError_t launch_field_rc(bool two_d, bool mixed, const SnFieldArgs &args, int grid, int smem_bytes,
+cudaError_t launch_field_rc(bool two_d, bool mixed, const SnFieldArgs &args, int grid, int threads, int smem_bytes,
                             cudaStream_t st)
 {
     static bool configured[4] = {false, false, false, false};
@@ -640,12 +681,13 @@ cudaError_t launch_field_rc(bool two_d, bool mixed, const SnFieldArgs &args, int
         configured[idx] = true;
     }
     if (grid <= 0) return cudaSuccess;
-    fn<<<grid, SN_THREADS, smem_bytes, st>>>(args);
+    fn<<<grid, threads, smem_bytes, st>>>(args);
     return cudaGetLastError();
 }
 
 template <int RC>
-cudaError_t launch_rc(bool two_d, bool mixed, const SnPhaseArgs &args, int grid, int smem_bytes, cudaStream_t st)
+cudaError_t launch_rc(bool two_d, bool mixed, const SnPhaseArgs &args, int grid, int threads, int smem_bytes,
+                      cudaStream_t st)
 {
     static bool configured[4] = {false, false, false, false};
     const int idx = (two_d ? 2 : 0) + (mixed ? 1 : 0);
@@ -658,24 +700,26 @@ cudaError_t launch_rc(bool two_d, bool mixed, const SnPhaseArgs &args, int grid,
         configured[idx] = true;
     }
     if (grid <= 0) return cudaSuccess;
-    fn<<<grid, SN_THREADS, smem_bytes, st>>>(args);
+    fn<<<grid, threads, smem_bytes, st>>>(args);
     return cudaGetLastError();
 }
 
-// Sizes the host needs for planning (must match the kernel's template choices).
+// Compile-time sizes the host planner needs.
 template <int RC>
-inline void geo_sizes(bool two_d, int &S, int &SZ, int &NS, int &NF)
+inline void geo_sizes(bool two_d, int &S, int &SZ, int &NS, int &NF, int &merge)
 {
     if (two_d) {
         S = Geo<RC, true>::S;
         SZ = Geo<RC, true>::SZ;
         NS = Geo<RC, true>::NS;
         NF = Geo<RC, true>::NF;
+        merge = Geo<RC, true>::MERGE;
     } else {
         S = Geo<RC, false>::S;
         SZ = Geo<RC, false>::SZ;
         NS = Geo<RC, false>::NS;
         NF = Geo<RC, false>::NF;
+        merge = Geo<RC, false>::MERGE;
     }
 }
 

@@ -13,21 +13,21 @@
 
 static_assert(sizeof(SnFieldArgsHost) >= sizeof(sn_sweep::SnFieldArgs), "field args layout");
 
-cudaError_t SN_CAT(sn_launch_sweep_rc, SN_RC)(bool two_d, bool mixed, const SnPhaseArgs &a, int grid, int smem,
-                                              cudaStream_t st)
+cudaError_t SN_CAT(sn_launch_sweep_rc, SN_RC)(bool two_d, bool mixed, const SnPhaseArgs &a, int grid, int threads,
+                                              int smem, cudaStream_t st)
 {
-    return sn_sweep::launch_rc<SN_RC>(two_d, mixed, a, grid, smem, st);
+    return sn_sweep::launch_rc<SN_RC>(two_d, mixed, a, grid, threads, smem, st);
 }
 
 cudaError_t SN_CAT(sn_launch_field_rc, SN_RC)(bool fp64, bool two_d, bool mixed, const void *field_args, int grid,
-                                              int smem, cudaStream_t st)
+                                              int threads, int smem, cudaStream_t st)
 {
     const sn_sweep::SnFieldArgs &fa = *static_cast<const sn_sweep::SnFieldArgs *>(field_args);
-    if (fp64) return sn_sweep::launch_field_rc<double, SN_RC>(two_d, mixed, fa, grid, smem, st);
-    return sn_sweep::launch_field_rc<float, SN_RC>(two_d, mixed, fa, grid, smem, st);
+    if (fp64) return sn_sweep::launch_field_rc<double, SN_RC>(two_d, mixed, fa, grid, threads, smem, st);
+    return sn_sweep::launch_field_rc<float, SN_RC>(two_d, mixed, fa, grid, threads, smem, st);
 }
 
-void SN_CAT(sn_geo_rc, SN_RC)(bool two_d, int *S, int *SZ, int *NS, int *NF)
+void SN_CAT(sn_geo_rc, SN_RC)(bool two_d, int *S, int *SZ, int *NS, int *NF, int *merge)
 {
-    sn_sweep::geo_sizes<SN_RC>(two_d, *S, *SZ, *NS, *NF);
+    sn_sweep::geo_sizes<SN_RC>(two_d, *S, *SZ, *NS, *NF, *merge);
 }

@@ -90,6 +90,13 @@ def check_schedule(X: int, Y: int, Z: int, cutoff: int, sched: dict) -> bool:
     return bool(lib().sn_check_schedule(X, Y, Z, cutoff, ctypes.byref(info)))
 
 
+def fp32_peak():
+    """(measured FP32 TFLOP/s on the current device, nominal max SM clock MHz)."""
+    t, c = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    check(lib().sn_gpu_fp32_peak(ctypes.byref(t), ctypes.byref(c)))
+    return t.value, c.value
+
+
 def neighbour_count(cutoff: int, Z: int) -> int:
     return lib().sn_neighbour_count(cutoff, Z)
 
@@ -270,6 +277,12 @@ class Simulation:
 
     def stream_ptr(self) -> int:
         return lib().sn_gpu_stream(self._h) or 0
+
+    def phase_times(self, n_sweeps: int = 3):
+        """(mean ms of one block-colour launch, mean ms per sweep, launches per sweep)."""
+        a, b, n = ctypes.c_double(0.0), ctypes.c_double(0.0), ctypes.c_int(0)
+        self._ck(lib().sn_gpu_phase_times(self._h, int(n_sweeps), ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)))
+        return a.value, b.value, n.value
 
     def proposals(self, replica: int, sites: np.ndarray, sweep: int) -> np.ndarray:
         sites = np.ascontiguousarray(sites, np.uint32)
