@@ -204,6 +204,30 @@ sn_status sn_gpu_adjoint(sn_handle *h, int replica, float *dE_dp, double *dE_dpa
  * (nullable, n_steps+1 doubles) receives E before and after each step. */
 sn_status sn_gpu_quench(sn_handle *h, int replica, int n_steps, float step, double *E_trace);
 
+/* ---- energy without device allocation -------------------------------------------
+ * No counterpart in the reference, which has no library API at all.  For
+ * callers that may not allocate device memory (a plugin whose host framework
+ * owns the device memory pool, a process that has reserved nearly all device
+ * memory for its lattices, a long run that must not risk an out-of-memory
+ * failure between sweeps): the total energy of a lattice held in the
+ * CALLER's device memory -- d_px, d_py, d_pz, d_len are device pointers to
+ * N = X*Y*Z floats each, index (x*Y+y)*Z+z, vacancies as zero vectors of
+ * length 0 -- computed like sn_gpu_energy(SN_ENERGY_FP32) without any device
+ * allocation.  efield may be NULL (params->efield is used); *E_total is a
+ * host double; stream is a cudaStream_t or NULL (the default stream), and the
+ * call returns after the result is on the host.
+ * All scratch lives in one fixed device array inside the library (about
+ * 1 MiB, on every GPU that loads it, until exit): the lattice may split into
+ * at most 65536 tiles (512^3 at cutoff 3 needs 32768); larger lattices are
+ * rejected with SN_ERR_ARG.  Every call reuses that array, so calls whose GPU
+ * work overlaps race and return wrong energies: keep them ordered on one
+ * stream.  The first call on each device looks up the array's device
+ * address (with that device current) and should come before any stream
+ * capture begins. */
+sn_status sn_gpu_energy_noalloc(const float *d_px, const float *d_py, const float *d_pz, const float *d_len,
+                                int X, int Y, int Z, const sn_params *params, const float *efield,
+                                double *E_total, void *stream);
+
 /* ---- random streams ---------------------------------------------------------- */
 
 /* Philox4x32-10 of n (counter, key) pairs on the device: ctr 4n words,

@@ -106,6 +106,7 @@ def lib() -> ctypes.CDLL:
             "sn_neighbour_count": ([_i, _i], _i),
             "sn_gpu_philox": ([_vp, _vp, _vp, _i], _i),
             "sn_gpu_fp32_peak": ([_P(ctypes.c_double), _P(ctypes.c_double)], _i),
+            "sn_gpu_energy_noalloc": ([_vp, _vp, _vp, _vp, _i, _i, _i, _P(Params), _vp, _P(ctypes.c_double), _vp], _i),
             "sn_gpu_phase_times": ([h, _i, _P(ctypes.c_double), _P(ctypes.c_double), _P(_i)], _i),
             "sn_gpu_proposals": ([h, _i, _vp, _i, ctypes.c_uint32, _vp], _i),
         }

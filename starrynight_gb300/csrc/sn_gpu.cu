@@ -249,6 +249,24 @@ void fill_info(const SnTile &t, int rc, sn_schedule_info *o)
 
 }  // namespace
 
+// Internal helpers shared with the no-allocation entry point (sn_noalloc.cu).
+void sn_internal_set_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
+bool sn_internal_plan(int X, int Y, int Z, int rc, bool mixed, SnTile *out, char *why, size_t why_len)
+{
+    std::string w;
+    const bool ok = plan_tile(X, Y, Z, rc, mixed, *out, w);
+    if (!ok && why && why_len) snprintf(why, why_len, "%s", w.c_str());
+    return ok;
+}
+
+cudaError_t sn_internal_field_launch(int rc, bool fp64, bool two_d, bool mixed, const SnFieldArgsHost &a, int grid,
+                                     int threads, int smem, cudaStream_t st)
+{
+    if (rc < 1 || rc > SN_MAX_CUTOFF) return cudaErrorInvalidValue;
+    return k_field[rc](fp64, two_d, mixed, &a, grid, threads, smem, st);
+}
+
 // ---------------------------------------------------------------------------
 struct sn_handle {
     sn_params params{};

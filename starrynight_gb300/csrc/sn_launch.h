@@ -65,6 +65,12 @@ struct SnInitArgs {
 };
 
 cudaError_t sn_launch_init_lattice(const SnInitArgs &a, cudaStream_t st);
+
+// Planner, field-pass launcher and error slot of sn_gpu.cu, for sn_noalloc.cu.
+void sn_internal_set_error(const char *msg);
+bool sn_internal_plan(int X, int Y, int Z, int rc, bool mixed, SnTile *out, char *why, size_t why_len);
+cudaError_t sn_internal_field_launch(int rc, bool fp64, bool two_d, bool mixed, const SnFieldArgsHost &a, int grid,
+                                     int threads, int smem, cudaStream_t st);
 cudaError_t sn_launch_upload_convert(const float *stage_xyz, const float *stage_len, float *px, float *py, float *pz,
                                      float *len, long long n, float uniform_len, int mixed, float default_len,
                                      int *flags, cudaStream_t st);

@@ -60,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             obj = os.path.join(LIBDIR, "sn_sweep_rc%d.o" % rc)
             jobs.append([NVCC] + ARCH + NVFLAGS + ["-DSN_RC=%d" % rc, "-c", os.path.join(CSRC, "sn_sweep_inst.cu"),
                                                    "-o", obj])
-        for name in ("sn_kernels", "sn_gpu"):
+        for name in ("sn_kernels", "sn_gpu", "sn_noalloc"):
             jobs.append([NVCC] + ARCH + NVFLAGS + ["-c", os.path.join(CSRC, name + ".cu"),
                                                    "-o", os.path.join(LIBDIR, name + ".o")])
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
