@@ -54,8 +54,8 @@ typedef struct sn_params {
     int cutoff;                      /* DipoleCutOff (lattice units)                    */
     int dim;                         /* 3: sphere proposals; 2: circle (DIM<3 branch)   */
     int constrain_to_x;              /* ConstrainToX: proposals along +-x,+-y,+-z       */
-    float cage_strain;               /* CageStrain                                      */
-    float K;                         /* K, epitaxial term; applied only when K > 0      */
+    double cage_strain;              /* CageStrain (double, as the reference holds it)  */
+    double K;                        /* K, epitaxial term; applied only when K > 0      */
     float efield[3];                 /* Efield.{x,y,z}; replicas may override           */
     int n_species;                   /* length of Dipoles / Prevalence                  */
     float dipoles[SN_MAX_SPECIES];   /* Dipoles: species lengths (0 = vacancy)          */

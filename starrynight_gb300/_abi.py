@@ -34,7 +34,7 @@ class SnError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [
         ("cutoff", ctypes.c_int), ("dim", ctypes.c_int), ("constrain_to_x", ctypes.c_int),
-        ("cage_strain", ctypes.c_float), ("K", ctypes.c_float), ("efield", ctypes.c_float * 3),
+        ("cage_strain", ctypes.c_double), ("K", ctypes.c_double), ("efield", ctypes.c_float * 3),
         ("n_species", ctypes.c_int), ("dipoles", ctypes.c_float * SN_MAX_SPECIES),
         ("prevalence", ctypes.c_float * SN_MAX_SPECIES), ("seed", ctypes.c_uint64),
     ]

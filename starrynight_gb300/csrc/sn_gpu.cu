@@ -411,8 +411,8 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
             a.geoms = h->d_geoms;
             a.acc = h->d_acc;
             a.sweep = h->d_sweep;
-            a.cage = h->params.cage_strain;
-            a.K = h->params.K;
+            a.cage = (float)h->params.cage_strain;
+            a.K = (float)h->params.K;
             a.constrain = h->params.constrain_to_x;
             a.dim = h->params.dim;
             if (events && ev + 1 < events->size()) e = cudaEventRecord((*events)[ev++], h->stream);

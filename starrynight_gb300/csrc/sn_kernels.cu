@@ -139,9 +139,9 @@ __global__ void sweep_end_kernel(SnAccum *acc, SnState *state, double *hist, SnR
 
 // red (10 doubles, see SnFieldArgs) -> running E and P of one replica.
 __global__ void recompute_finish_kernel(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
-                                        float cage, double *drift_max, int record)
+                                        double cage, double *drift_max, int record)
 {
-    const double E = red[0] - 0.5 * (double)cage * red[1] + red[2] + red[3];
+    const double E = red[0] - 0.5 * cage * red[1] + red[2] + red[3];
     SnState &s = state[rep];
     if (record) {
         const double d = fabs(s.E - E) / fmax(fabs(E), 1.0);
@@ -259,7 +259,7 @@ cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnRe
 }
 
 cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
-                                       float cage, double *drift_max, int record, cudaStream_t st)
+                                       double cage, double *drift_max, int record, cudaStream_t st)
 {
     recompute_finish_kernel<<<1, 1, 0, st>>>(red, state, reps, rep, cage, drift_max, record);
     return cudaGetLastError();

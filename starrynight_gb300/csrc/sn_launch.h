@@ -36,8 +36,8 @@ struct SnFieldArgsHost {
     const SnWork *work;
     const SnReplicaDev *reps;
     const SnTile *geoms;
-    float cage;
-    float K;
+    double cage;
+    double K;
     double *site_e;
     float *grad;
     double *red;
@@ -79,7 +79,7 @@ cudaError_t sn_launch_download_convert(const float *px, const float *py, const f
 cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnReplicaDev *reps, int nrep,
                                 uint32_t *sweep, SnExchange *ex, int *order, cudaStream_t st);
 cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
-                                       float cage, double *drift_max, int record, cudaStream_t st);
+                                       double cage, double *drift_max, int record, cudaStream_t st);
 cudaError_t sn_launch_quench_step(float *px, float *py, float *pz, const float *len, const float *grad,
                                   long long n, float step, cudaStream_t st);
 cudaError_t sn_launch_fma_peak(float *out, int blocks, int threads, int iters, cudaStream_t st);

@@ -81,7 +81,19 @@ __device__ __forceinline__ void pair_step(const unsigned char *__restrict__ base
     const float *pb = reinterpret_cast<const float *>(base + ((int)tb + bo) - 12 * o.z);
     const R ax = pa[0], ay = pa[1], az = pa[2];
     const R bx = pb[0], by = pb[1], bz = pb[2];
-    const R qx = ax + bx, qy = ay + by, qz = az + bz;
+    R qx, qy, qz;
+    if constexpr (MIXED) {
+        // the tile holds unit p; weight each neighbour by its length here,
+        // in the accumulator's precision
+        const R la = tlen[(int)tslot + ao / 12 + o.z], lb = tlen[(int)tslot + bo / 12 - o.z];
+        qx = sn_fma(la, ax, lb * bx);
+        qy = sn_fma(la, ay, lb * by);
+        qz = sn_fma(la, az, lb * bz);
+    } else {
+        qx = ax + bx;
+        qy = ay + by;
+        qz = az + bz;
+    }
     constexpr R txx = (R)sn_stencil::tensor_d(o.x, o.y, o.z, 0);
     constexpr R tyy = (R)sn_stencil::tensor_d(o.x, o.y, o.z, 1);
     constexpr R tzz = (R)sn_stencil::tensor_d(o.x, o.y, o.z, 2);
@@ -99,13 +111,11 @@ __device__ __forceinline__ void pair_step(const unsigned char *__restrict__ base
     if constexpr (tyz != 0.0f) a[2] = sn_fma(tyz, qy, a[2]);
     a[2] = sn_fma(tzz, qz, a[2]);
     if constexpr (o.x * o.x + o.y * o.y + o.z * o.z == 1) {
+        // cage strain: unweighted sum of the six nearest dipoles
         if constexpr (MIXED) {
-            // the tile holds len*p; the cage-strain term wants unit p
-            const R la = tlen[(int)tslot + ao / 12 + o.z], lb = tlen[(int)tslot + bo / 12 - o.z];
-            const R ia = la > R(0) ? R(1) / la : R(0), ib = lb > R(0) ? R(1) / lb : R(0);
-            nn[0] += ax * ia + bx * ib;
-            nn[1] += ay * ia + by * ib;
-            nn[2] += az * ia + bz * ib;
+            nn[0] += ax + bx;
+            nn[1] += ay + by;
+            nn[2] += az + bz;
         } else {
             nn[0] += qx;
             nn[1] += qy;
@@ -275,21 +285,6 @@ __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &
     }
 }
 
-// The tile of a mixed-length lattice holds len * p.
-template <bool MIXED>
-__device__ __forceinline__ void scale_tile(float *tile, const float *tlen, int slots, int tid, int nthreads)
-{
-    if constexpr (MIXED) {
-        for (int i = tid; i < slots; i += nthreads) {
-            const float L = tlen[i];
-            tile[3 * i + 0] *= L;
-            tile[3 * i + 1] *= L;
-            tile[3 * i + 2] *= L;
-        }
-        __syncthreads();
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Sweep kernel.  Thread tid owns split j = tid / tg of the stencil for target
 // tt = tid % tg of every colour group: half h = tt / tp of the group, target
@@ -393,7 +388,6 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseAr
             }
             if (g == 0) cp_async_wait_all();
             __syncthreads();
-            if (g == 0) scale_tile<MIXED>(tile, tlen, Gm.slots, tid, nthreads);
         }
 
         int cx, cy, cz;
@@ -441,26 +435,16 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseAr
                     gz += pp[2 * tg];
                 }
                 const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + (TWO_D ? 0 : w.z0 + cz) + srel;
-                float Li, ox, oy, oz;
-                if constexpr (MIXED) {
-                    Li = tlen[tslot];
-                    ox = gpx[site];
-                    oy = gpy[site];
-                    oz = gpz[site];
-                } else {
-                    Li = Lu;
-                    ox = tile[3 * tslot + 0];
-                    oy = tile[3 * tslot + 1];
-                    oz = tile[3 * tslot + 2];
-                }
+                const float Li = MIXED ? tlen[tslot] : Lu;
+                const float ox = tile[3 * tslot + 0], oy = tile[3 * tslot + 1], oz = tile[3 * tslot + 2];
                 const float dx = pr.x - ox, dy = pr.y - oy, dz = pr.z - oz;
                 float dE = fmaf(dx, gx, fmaf(dy, gy, dz * gz));
                 if (Kk > 0.0f) dE -= Kk * ((fabsf(pr.x) - fabsf(ox)) + (fabsf(pr.y) - fabsf(oy)));
                 satt++;
                 if (dE < pr.w) {
-                    tile[3 * tslot + 0] = MIXED ? Li * pr.x : pr.x;
-                    tile[3 * tslot + 1] = MIXED ? Li * pr.y : pr.y;
-                    tile[3 * tslot + 2] = MIXED ? Li * pr.z : pr.z;
+                    tile[3 * tslot + 0] = pr.x;
+                    tile[3 * tslot + 1] = pr.y;
+                    tile[3 * tslot + 2] = pr.z;
                     gpx[site] = pr.x;
                     gpy[site] = pr.y;
                     gpz[site] = pr.z;
@@ -508,8 +492,8 @@ struct SnFieldArgs {
     const SnWork *work;
     const SnReplicaDev *reps;
     const SnTile *geoms;
-    float cage;
-    float K;
+    double cage;
+    double K;
     double *site_e;  // nullable: N doubles
     float *grad;     // nullable: 3N floats (interleaved)
     double *red;     // 10 doubles per replica
@@ -554,7 +538,6 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
     stage_tile<RC, TWO_D, MIXED>(Rp, Gm, w, tile, tlen, start, tid, nthreads);
     cp_async_wait_all();
     __syncthreads();
-    scale_tile<MIXED>(tile, tlen, Gm.slots, tid, nthreads);
 
     const int j = tid / tg, tt = tid - (tid / tg) * tg;
     const int hh = tt / tp, t = tt - (tt / tp) * tp;
@@ -611,7 +594,7 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
             }
             const long long site = ((long long)(w.x0 + cx) * Y + (w.y0 + cy)) * Z + (TWO_D ? 0 : w.z0 + cz) + srel;
             const double px = gpx[site], py = gpy[site], pz = gpz[site];
-            const double Li = MIXED ? (double)glen[site] : (double)Rp.length;
+            const double Li = (double)glen[site];  // 0 at vacancies in both modes
             if (Li == 0.0) {
                 if (a.site_e) a.site_e[site] = 0.0;
                 if (a.grad) {
