@@ -776,7 +776,6 @@ sn_status sn_gpu_upload_lattice(sn_handle *h, int replica, const float *xyz, con
     if (flags[0])
         return fail(h, SN_ERR_ARG, "upload has a dipole length other than %g, but the handle was created for a single "
                                    "species length (list every species in sn_params.dipoles)", (double)h->length);
-    if (flags[1]) return fail(h, SN_ERR_ARG, "an occupied site (length > 0) holds the zero vector");
     return SN_OK;
 }
 

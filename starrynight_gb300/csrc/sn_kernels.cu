@@ -46,8 +46,9 @@ __global__ void init_lattice_kernel(const SnInitArgs a)
 }
 
 // flags[0]: a length that differs from the uniform length (uniform mode)
-// flags[1]: an occupied site holding the zero vector
 // flags[2]: a negative or non-finite length
+// (an occupied site may hold any orientation, the zero vector included, as
+// the reference's buckled and slab_delete patterns produce)
 __global__ void upload_convert_kernel(const float *__restrict__ sxyz, const float *__restrict__ slen, float *px,
                                       float *py, float *pz, float *len, long long n, float uniform_len, int mixed,
                                       float default_len, int *flags)
@@ -61,7 +62,6 @@ __global__ void upload_convert_kernel(const float *__restrict__ sxyz, const floa
             x = y = z = 0.0f;
         } else {
             if (!mixed && L != uniform_len) atomicOr(&flags[0], 1);
-            if (x == 0.0f && y == 0.0f && z == 0.0f) atomicOr(&flags[1], 1);
         }
         px[i] = x;
         py[i] = y;

@@ -74,7 +74,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     drv = driver_path()
     dsrc = [os.path.join(PKG, "driver", "starrynight-gpu.c"), os.path.join(PKG, "cfg", "libconfig_min.c")]
     if all(os.path.exists(p) for p in dsrc) and (force or _stale(drv, dsrc + [so])):
-        _run(["gcc", "-O2", "-std=c11", "-Wall", "-I" + INCLUDE, "-I" + os.path.join(PKG, "cfg"), "-o", drv] + dsrc +
+        _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-I" + INCLUDE, "-I" + os.path.join(PKG, "cfg"), "-o", drv] + dsrc +
              ["-L" + LIBDIR, "-lsn_gpu", "-Wl,-rpath,$ORIGIN", "-lm"])
     return so
 

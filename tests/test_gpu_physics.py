@@ -257,7 +257,7 @@ def test_errors_are_statuses_not_exits(native_lib):
             sim.upload(0, xyz, np.full(512, 0.5, np.float32))  # a length the handle does not know
         assert e.value.name == "SN_ERR_ARG"
         with pytest.raises(sn.SnError) as e:
-            sim.upload(0, np.zeros((512, 3), np.float32), np.ones(512, np.float32))  # occupied zero vectors
+            sim.upload(0, xyz, np.full(512, -1.0, np.float32))  # negative lengths
         assert e.value.name == "SN_ERR_ARG"
         with pytest.raises(sn.SnError):
             sim.set_temperature(3, 100.0)
