@@ -149,6 +149,11 @@ sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *r
 /* Total sweeps done so far (the Philox sweep counter). */
 sn_status sn_gpu_sweep_count(const sn_handle *h, uint64_t *sweeps);
 
+/* Sets the sweep counter (what sn_gpu_sweep_count reports and what keys the
+ * sweep's random stream) -- used to resume from a checkpoint so that the
+ * continued run is the run that never stopped.  No reference counterpart. */
+sn_status sn_gpu_set_sweep_count(sn_handle *h, uint64_t sweeps);
+
 /* ---- energies and observables -------------------------------------------- */
 
 /* Full recompute of one replica's energy (FP64 total).  site_E (nullable,
@@ -203,6 +208,34 @@ sn_status sn_gpu_adjoint(sn_handle *h, int replica, float *dE_dp, double *dE_dpa
  * p <- normalize(p - step (g - (g.p) p)) at every occupied site.  E_trace
  * (nullable, n_steps+1 doubles) receives E before and after each step. */
 sn_status sn_gpu_quench(sn_handle *h, int replica, int n_steps, float step, double *E_trace);
+
+/* ---- analysis on the resident lattice ------------------------------------
+ * The per-site maps and order parameters of src/starrynight-analysis.c,
+ * computed on the device; the caller's buffers are host memory.
+ *
+ * sn_gpu_potential: dipole_potential(x,y,z) (:65-94, called with MAX = 6 by
+ *   every writer) for all N sites into pot[N], index (x*Y+y)*Z+z.  Bit-equal
+ *   to the reference's value (same float terms, same double sum order).
+ * sn_gpu_efield: |E| of dipole_electricfield(cutoff,x,y,z) (:393-450, cutoff 4
+ *   in lattice_Efield_XYZ) or, with half_offset = 1, of
+ *   dipole_electricfieldoffset (:310-380, cutoff 2 in
+ *   lattice_Efieldoffset_XYZ) for all sites into magnitude[N]; bit-equal.
+ * sn_gpu_radial_order: the histograms of radial_order_parameter (:528-598,
+ *   cutoff 9): per bin b = |r|^2 in [0, cutoff^2], fe_sum[b] = sum over sites
+ *   and offsets of p_i.p_j, afe_sum[b] = sum of p_i.p_j - 3(n.p_i)(n.p_j),
+ *   count[b] = number of terms; arrays of cutoff^2+1 entries (any may be
+ *   NULL).  Summed in FP64 (the reference sums in float).
+ * sn_gpu_order_parameters: polarisation() (:48-62) = sum p_x / N and
+ *   landau_order() (:506-526) = |sum p|^2, both unweighted by length, and the
+ *   orientation sum itself (orientation_sum[3]); any output may be NULL.
+ * Cutoffs are limited to 1..32.  Lattice sides shorter than the cutoff wrap
+ * periodically (the reference indexes out of bounds there). */
+sn_status sn_gpu_potential(sn_handle *h, int replica, int cutoff, double *pot);
+sn_status sn_gpu_efield(sn_handle *h, int replica, int cutoff, int half_offset, double *magnitude);
+sn_status sn_gpu_radial_order(sn_handle *h, int replica, int cutoff, double *fe_sum, double *afe_sum,
+                              int64_t *count);
+sn_status sn_gpu_order_parameters(sn_handle *h, int replica, double *polarisation_x, double *landau,
+                                  double *orientation_sum);
 
 /* ---- energy without device allocation -------------------------------------------
  * No counterpart in the reference, which has no library API at all.  For

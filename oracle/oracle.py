@@ -38,6 +38,7 @@ def lib() -> ctypes.CDLL:
             build()
         _LIB = ctypes.CDLL(path)
         _declare(_LIB)
+        _declare_analysis(_LIB)
     return _LIB
 
 
@@ -72,6 +73,7 @@ _d = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 _i = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _u32 = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_i64 = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _vp = ctypes.c_void_p
 _P = ctypes.POINTER
 
@@ -103,6 +105,13 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sno_energy64.restype = ctypes.c_double
     L.sno_delta_energy64.argtypes = [_P(Model), _f, _f, _f, _f, ctypes.c_int, _f]
     L.sno_delta_energy64.restype = ctypes.c_double
+
+
+def _declare_analysis(L: ctypes.CDLL) -> None:
+    L.sno_potential_map.argtypes = [_f, _f, _f, _f] + [ctypes.c_int] * 4 + [_d]
+    L.sno_efield_map.argtypes = [_f, _f, _f] + [ctypes.c_int] * 5 + [_d]
+    L.sno_radial_order.argtypes = [_f, _f, _f] + [ctypes.c_int] * 5 + [_d, _d, _i64]
+    L.sno_order_params.argtypes = [_f, _f, _f, ctypes.c_longlong, _P(ctypes.c_double), _P(ctypes.c_double), _d]
 
 
 def _ptr(a):
@@ -244,3 +253,44 @@ def delta_energy64(m: Model, px, py, pz, length, site: int, newp) -> float:
 def soa(lat4: np.ndarray):
     """AoS (x,y,z,len) -> four contiguous float32 arrays."""
     return tuple(np.ascontiguousarray(lat4[:, k]) for k in range(4))
+
+
+# ---- analysis (src/starrynight-analysis.c) ----
+
+def _soa3(px, py, pz):
+    return [np.ascontiguousarray(a, np.float32).reshape(-1) for a in (px, py, pz)]
+
+
+def potential_map(px, py, pz, length, shape, cutoff: int = 6) -> np.ndarray:
+    """dipole_potential at every site (bit-equal to the reference)."""
+    X, Y, Z = shape
+    out = np.zeros(X * Y * Z, np.float64)
+    a = _soa3(px, py, pz)
+    lib().sno_potential_map(*a, np.ascontiguousarray(length, np.float32).reshape(-1), X, Y, Z, int(cutoff), out)
+    return out
+
+
+def efield_map(px, py, pz, shape, cutoff: int = 4, half: bool = False) -> np.ndarray:
+    """|E| of dipole_electricfield (half=False) or dipole_electricfieldoffset (half=True)."""
+    X, Y, Z = shape
+    out = np.zeros(X * Y * Z, np.float64)
+    lib().sno_efield_map(*_soa3(px, py, pz), X, Y, Z, int(cutoff), int(bool(half)), out)
+    return out
+
+
+def radial_order(px, py, pz, shape, cutoff: int = 9, float_sums: bool = False):
+    """(fe_sum, afe_sum, count) per |r|^2 bin of radial_order_parameter: FP64 sums, or the
+    reference's own float sums with float_sums=True."""
+    X, Y, Z = shape
+    nb = cutoff * cutoff + 1
+    fe, afe, cnt = np.zeros(nb), np.zeros(nb), np.zeros(nb, np.int64)
+    lib().sno_radial_order(*_soa3(px, py, pz), X, Y, Z, int(cutoff), int(bool(float_sums)), fe, afe, cnt)
+    return fe, afe, cnt
+
+
+def order_params(px, py, pz):
+    """(polarisation_x, landau, orientation sum[3]) of polarisation() / landau_order()."""
+    a = _soa3(px, py, pz)
+    pol, lan, s3 = ctypes.c_double(0.0), ctypes.c_double(0.0), np.zeros(3)
+    lib().sno_order_params(*a, a[0].size, ctypes.byref(pol), ctypes.byref(lan), s3)
+    return pol.value, lan.value, s3

@@ -188,3 +188,92 @@ EXPORT void refh_observables(double *pol_x, double *landau)
 }
 
 EXPORT unsigned int refh_mt_next(void) { return (unsigned int)genrand_int32(); }
+
+/* ---- analysis entry points: the reference's own functions on the current
+ * lattice (src/starrynight-analysis.c). ---- */
+
+/* Orientation patterns of src/starrynight-lattice.c:39-137 by InitialLattice
+ * name (what main() selects, src/starrynight-main.c:180-200); lengths untouched. */
+EXPORT int refh_init_pattern(const char *name)
+{
+    if (!strcmp(name, "random")) initialise_lattice_random();
+    else if (!strcmp(name, "ferroelectric")) initialise_lattice_ferroelectric();
+    else if (!strcmp(name, "buckled")) initialise_lattice_buckled();
+    else if (!strcmp(name, "antiferro_wall")) initialise_lattice_antiferro_wall();
+    else if (!strcmp(name, "ferro_wall")) initialise_lattice_ferro_wall();
+    else if (!strcmp(name, "antiferro_slip")) initialise_lattice_antiferro_slip();
+    else if (!strcmp(name, "spectrum")) initialise_lattice_spectrum();
+    else if (!strcmp(name, "slab_delete")) initialise_lattice_slab_delete();
+    else return -1;
+    return 0;
+}
+
+/* dipole_potential (:65-94) at every site, index (x*Y+y)*Z+z */
+EXPORT void refh_potential_map(double *out)
+{
+    int x, y, z;
+    for (x = 0; x < X; x++)
+        for (y = 0; y < Y; y++)
+            for (z = 0; z < Z; z++) out[((long)x * Y + y) * Z + z] = dipole_potential(x, y, z);
+}
+
+/* |E| of dipole_electricfield (:393-450) or, half = 1, of
+ * dipole_electricfieldoffset (:310-380; its per-term stderr trace muted) */
+EXPORT void refh_efield_map(int cutoff, int half, double *out)
+{
+    int x, y, z;
+    if (half) mute();
+    for (x = 0; x < X; x++)
+        for (y = 0; y < Y; y++)
+            for (z = 0; z < Z; z++)
+                out[((long)x * Y + y) * Z + z] =
+                    half ? dipole_electricfieldoffset(cutoff, x, y, z) : dipole_electricfield(cutoff, x, y, z);
+    if (half) unmute();
+}
+
+/* The reference's writers, by name, on the current lattice. */
+EXPORT int refh_write(const char *kind, const char *path)
+{
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s", path);
+    if (!strcmp(kind, "potential_xyz")) lattice_potential_XYZ(buf);
+    else if (!strcmp(kind, "potential_cube")) lattice_potential_cube(buf);
+    else if (!strcmp(kind, "efield_xyz")) lattice_Efield_XYZ(buf);
+    else if (!strcmp(kind, "efieldoffset_xyz")) {
+        mute();
+        lattice_Efieldoffset_XYZ(buf);
+        unmute();
+    } else if (!strcmp(kind, "potential_pgm")) outputpotential_png(buf);
+    else if (!strcmp(kind, "dipoles_xyz")) outputlattice_xyz(buf);
+    else if (!strcmp(kind, "dipoles_ppm")) outputlattice_ppm_hsv(buf);
+    else if (!strcmp(kind, "dipoles_svg")) outputlattice_svg(buf);
+    else if (!strcmp(kind, "rdf")) radial_order_parameter(buf);
+    else if (!strcmp(kind, "recombination")) {
+        FILE *fo = fopen(buf, "w");
+        if (!fo) return -2;
+        mute();
+        recombination_calculator(fo);
+        unmute();
+        fclose(fo);
+    } else return -1;
+    fflush(NULL); /* outputlattice_xyz leaves its file open */
+    return 0;
+}
+
+/* stderr output of outputlattice_dumb_terminal (:820-925) or of
+ * recombination_calculator(stderr) (:97-230, as analysis_initial calls it)
+ * captured into a file */
+EXPORT int refh_capture(const char *kind, const char *path)
+{
+    int saved, rc = 0;
+    fflush(stderr);
+    saved = dup(2);
+    if (saved < 0 || freopen(path, "w", stderr) == NULL) return -2;
+    if (!strcmp(kind, "dumb_terminal")) outputlattice_dumb_terminal();
+    else if (!strcmp(kind, "recombination")) recombination_calculator(stderr);
+    else rc = -1;
+    fflush(stderr);
+    dup2(saved, 2);
+    close(saved);
+    return rc;
+}

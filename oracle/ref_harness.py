@@ -18,6 +18,7 @@ _LIB = None
 
 _f = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _i = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_d = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 
 def available() -> bool:
@@ -42,6 +43,14 @@ def lib() -> ctypes.CDLL:
         L.refh_neighbours.restype = ctypes.c_int
         L.refh_observables.argtypes = [ctypes.POINTER(ctypes.c_double)] * 2
         L.refh_mt_next.restype = ctypes.c_uint
+        L.refh_init_pattern.argtypes = [ctypes.c_char_p]
+        L.refh_init_pattern.restype = ctypes.c_int
+        L.refh_potential_map.argtypes = [_d]
+        L.refh_efield_map.argtypes = [ctypes.c_int, ctypes.c_int, _d]
+        L.refh_write.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        L.refh_write.restype = ctypes.c_int
+        L.refh_capture.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        L.refh_capture.restype = ctypes.c_int
         _LIB = L
     return _LIB
 
@@ -93,3 +102,28 @@ class RefSim:
         a, b = ctypes.c_double(0.0), ctypes.c_double(0.0)
         lib().refh_observables(ctypes.byref(a), ctypes.byref(b))
         return a.value, b.value
+
+    def init_pattern(self, name: str) -> None:
+        """The reference's InitialLattice pattern (src/starrynight-lattice.c:39-137); lengths untouched."""
+        if lib().refh_init_pattern(name.encode()) != 0:
+            raise ValueError("unknown pattern %r" % name)
+
+    def potential_map(self) -> np.ndarray:
+        out = np.zeros(int(np.prod(self.shape)), np.float64)
+        lib().refh_potential_map(out)
+        return out
+
+    def efield_map(self, cutoff: int, half: bool = False) -> np.ndarray:
+        out = np.zeros(int(np.prod(self.shape)), np.float64)
+        lib().refh_efield_map(int(cutoff), int(bool(half)), out)
+        return out
+
+    def write(self, kind: str, path: str) -> None:
+        """One of the reference's writers (src/starrynight-analysis.c) on the current lattice."""
+        if lib().refh_write(kind.encode(), path.encode()) != 0:
+            raise ValueError("writer %r failed" % kind)
+
+    def capture(self, kind: str, path: str) -> None:
+        """stderr of outputlattice_dumb_terminal / recombination_calculator(stderr) into path."""
+        if lib().refh_capture(kind.encode(), path.encode()) != 0:
+            raise ValueError("capture %r failed" % kind)

@@ -629,3 +629,176 @@ double sno_energy64(const sno_model *m, const float *px, const float *py, const 
     tab64_free(&t);
     return E;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Analysis maps and order parameters (src/starrynight-analysis.c).          */
+
+/* dot() of src/starrynight-config.c:189-199: float sum from 0, x then y then z */
+static float an_dot(float ax, float ay, float az, float bx, float by, float bz)
+{
+    float s = 0.0f;
+    s += ax * bx;
+    s += ay * by;
+    s += az * bz;
+    return s;
+}
+
+static long an_wrap(int v, int L)
+{
+    v %= L;
+    return v < 0 ? v + L : v;
+}
+
+/* dipole_potential, src/starrynight-analysis.c:65-94 */
+void sno_potential_map(const float *px, const float *py, const float *pz, const float *len, int X, int Y, int Z,
+                       int cutoff, double *out)
+{
+    int x, y, z, dx, dy, dz;
+    for (x = 0; x < X; x++)
+        for (y = 0; y < Y; y++)
+            for (z = 0; z < Z; z++) {
+                double pot = 0.0;
+                for (dx = -cutoff; dx <= cutoff; dx++)
+                    for (dy = -cutoff; dy <= cutoff; dy++)
+                        for (dz = -cutoff; dz <= cutoff; dz++) {
+                            float rx, ry, rz, d, term;
+                            long j;
+                            if (dx == 0 && dy == 0 && dz == 0) continue;
+                            rx = (float)dx;
+                            ry = (float)dy;
+                            rz = (float)dz;
+                            d = (float)sqrt((double)(rx * rx + ry * ry + rz * rz));
+                            if (d > (float)cutoff) continue;
+                            j = (an_wrap(x + dx, X) * Y + an_wrap(y + dy, Y)) * Z + an_wrap(z + dz, Z);
+                            term = len[j] * an_dot(px[j], py[j], pz[j], rx, ry, rz) / (d * d * d);
+                            pot += term;
+                        }
+                out[((long)x * Y + y) * Z + z] = pot;
+            }
+}
+
+/* dipole_electricfield (half = 0), :393-450, and dipole_electricfieldoffset
+ * (half = 1), :310-380; returns |E| = sqrt(dot(E, E)) per site. */
+void sno_efield_map(const float *px, const float *py, const float *pz, int X, int Y, int Z, int cutoff, int half,
+                    double *out)
+{
+    const int lo = half ? -cutoff - 1 : -cutoff, hi = half ? cutoff - 1 : cutoff;
+    int x, y, z, dx, dy, dz;
+    for (x = 0; x < X; x++)
+        for (y = 0; y < Y; y++)
+            for (z = 0; z < Z; z++) {
+                const long i = ((long)x * Y + y) * Z + z;
+                float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+                for (dx = lo; dx <= hi; dx++)
+                    for (dy = lo; dy <= hi; dy++)
+                        for (dz = lo; dz <= hi; dz++) {
+                            float rx, ry, rz, d, nx, ny, nz, cx, cy, cz;
+                            double radial;
+                            long j;
+                            if (!half && dx == 0 && dy == 0 && dz == 0) continue;
+                            if (half) {
+                                rx = (float)dx + 0.5;
+                                ry = (float)dy + 0.5;
+                                rz = (float)dz + 0.5;
+                            } else {
+                                rx = (float)dx;
+                                ry = (float)dy;
+                                rz = (float)dz;
+                            }
+                            d = (float)sqrt((double)(rx * rx + ry * ry + rz * rz));
+                            if (d > (float)cutoff) continue;
+                            nx = rx / d;
+                            ny = ry / d;
+                            nz = rz / d;
+                            j = (an_wrap(x + dx, X) * Y + an_wrap(y + dy, Y)) * Z + an_wrap(z + dz, Z);
+                            radial = an_dot(nx, ny, nz, px[j], py[j], pz[j]);
+                            cx = 3 * nx * radial - px[j];
+                            cy = 3 * ny * radial - py[j];
+                            cz = 3 * nz * radial - pz[j];
+                            cx /= d * d * d;
+                            cy /= d * d * d;
+                            cz /= d * d * d;
+                            ex += cx;
+                            ey += cy;
+                            ez += cz;
+                        }
+                if (!half) {
+                    ex -= 1 / 3.0 * px[i];
+                    ey -= 1 / 3.0 * py[i];
+                    ez -= 1 / 3.0 * pz[i];
+                }
+                out[i] = sqrt(an_dot(ex, ey, ez, ex, ey, ez));
+            }
+}
+
+/* radial_order_parameter, :528-598; arrays of cutoff^2+1.  Bin sums in FP64,
+ * or with float_sums in float in the reference's order (its own histogram
+ * arithmetic, :576-577), returned as doubles. */
+#define SNO_MAX_BINS 1025
+void sno_radial_order(const float *px, const float *py, const float *pz, int X, int Y, int Z, int cutoff,
+                      int float_sums, double *fe, double *afe, long long *count)
+{
+    const int nb = cutoff * cutoff + 1;
+    static float ffe[SNO_MAX_BINS], fafe[SNO_MAX_BINS];
+    int x, y, z, dx, dy, dz, b;
+    if (nb > SNO_MAX_BINS) return;
+    for (b = 0; b < nb; b++) {
+        fe[b] = afe[b] = 0.0;
+        ffe[b] = fafe[b] = 0.0f;
+        count[b] = 0;
+    }
+    for (x = 0; x < X; x++)
+        for (y = 0; y < Y; y++)
+            for (z = 0; z < Z; z++) {
+                const long i = ((long)x * Y + y) * Z + z;
+                for (dx = -cutoff; dx <= cutoff; dx++)
+                    for (dy = -cutoff; dy <= cutoff; dy++)
+                        for (dz = -cutoff; dz <= cutoff; dz++) {
+                            const int ds = dx * dx + dy * dy + dz * dz;
+                            float c, a, d, nx, ny, nz;
+                            long j;
+                            if (ds > cutoff * cutoff) continue;
+                            j = (an_wrap(x + dx, X) * Y + an_wrap(y + dy, Y)) * Z + an_wrap(z + dz, Z);
+                            c = an_dot(px[i], py[i], pz[i], px[j], py[j], pz[j]);
+                            d = (float)sqrt((double)((float)dx * dx + dy * dy + dz * dz));
+                            if (d == 0) d = 1;
+                            nx = (float)dx / d;
+                            ny = (float)dy / d;
+                            nz = (float)dz / d;
+                            a = c - 3 * an_dot(nx, ny, nz, px[i], py[i], pz[i]) * an_dot(nx, ny, nz, px[j], py[j], pz[j]);
+                            if (float_sums) {
+                                ffe[ds] += c;
+                                fafe[ds] += a;
+                            } else {
+                                fe[ds] += c;
+                                afe[ds] += a;
+                            }
+                            count[ds]++;
+                        }
+            }
+    if (float_sums)
+        for (b = 0; b < nb; b++) {
+            fe[b] = ffe[b];
+            afe[b] = fafe[b];
+        }
+}
+
+/* polarisation() (:48-62) and landau_order() (:506-526), in FP64 */
+void sno_order_params(const float *px, const float *py, const float *pz, long long n, double *pol_x,
+                      double *landau, double *sum3)
+{
+    double s[3] = {0.0, 0.0, 0.0};
+    long long k;
+    for (k = 0; k < n; k++) {
+        s[0] += px[k];
+        s[1] += py[k];
+        s[2] += pz[k];
+    }
+    if (pol_x) *pol_x = s[0] / (double)n;
+    if (landau) *landau = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+    if (sum3) {
+        sum3[0] = s[0];
+        sum3[1] = s[1];
+        sum3[2] = s[2];
+    }
+}

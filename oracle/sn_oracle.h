@@ -133,3 +133,17 @@ double sno_delta_energy64(const sno_model *m, const float *px, const float *py, 
 #endif
 
 #endif
+
+/* ---- analysis (src/starrynight-analysis.c) ----------------------------------
+ * SoA lattice, index (x*Y+y)*Z+z.  Each follows the reference function it names
+ * statement by statement in float/double as the reference types them, so the
+ * per-site maps equal the reference's bit for bit; the histogram sums are
+ * FP64 (the reference's are float). */
+void sno_potential_map(const float *px, const float *py, const float *pz, const float *len, int X, int Y, int Z,
+                       int cutoff, double *out);
+void sno_efield_map(const float *px, const float *py, const float *pz, int X, int Y, int Z, int cutoff, int half,
+                    double *out);
+void sno_radial_order(const float *px, const float *py, const float *pz, int X, int Y, int Z, int cutoff,
+                      int float_sums, double *fe, double *afe, long long *count);
+void sno_order_params(const float *px, const float *py, const float *pz, long long n, double *pol_x,
+                      double *landau, double *sum3);

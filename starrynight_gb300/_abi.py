@@ -85,6 +85,7 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_download_lattice": ([h, _i, _vp, _vp], _i),
             "sn_gpu_sweep": ([h, _i, _P(ctypes.c_uint64), _P(ctypes.c_uint64)], _i),
             "sn_gpu_sweep_count": ([h, _P(ctypes.c_uint64)], _i),
+            "sn_gpu_set_sweep_count": ([h, ctypes.c_uint64], _i),
             "sn_gpu_energy": ([h, _i, _i, _P(ctypes.c_double), _vp], _i),
             "sn_gpu_observables": ([h, _vp, _vp, _vp], _i),
             "sn_gpu_history": ([h, _i, _i, _vp, _vp, _P(_i)], _i),
@@ -109,6 +110,10 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_energy_noalloc": ([_vp, _vp, _vp, _vp, _i, _i, _i, _P(Params), _vp, _P(ctypes.c_double), _vp], _i),
             "sn_gpu_phase_times": ([h, _i, _P(ctypes.c_double), _P(ctypes.c_double), _P(_i)], _i),
             "sn_gpu_proposals": ([h, _i, _vp, _i, ctypes.c_uint32, _vp], _i),
+            "sn_gpu_potential": ([h, _i, _i, _vp], _i),
+            "sn_gpu_efield": ([h, _i, _i, _i, _vp], _i),
+            "sn_gpu_radial_order": ([h, _i, _i, _vp, _vp, _vp], _i),
+            "sn_gpu_order_parameters": ([h, _i, _P(ctypes.c_double), _P(ctypes.c_double), _vp], _i),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/sn_gpu.h"
@@ -36,11 +37,20 @@ const sn_field_launch_fn k_field[SN_MAX_CUTOFF + 1] = {nullptr,
                                                         sn_launch_field_rc6};
 const sn_geo_fn k_geo[SN_MAX_CUTOFF + 1] = {nullptr,     sn_geo_rc1, sn_geo_rc2, sn_geo_rc3,
                                             sn_geo_rc4,  sn_geo_rc5, sn_geo_rc6};
+const sn_flow_launch_fn k_flow[SN_MAX_CUTOFF + 1] = {nullptr,
+                                                      sn_launch_flow_rc1,
+                                                      sn_launch_flow_rc2,
+                                                      sn_launch_flow_rc3,
+                                                      sn_launch_flow_rc4,
+                                                      sn_launch_flow_rc5,
+                                                      sn_launch_flow_rc6};
 
 const int kSmemLimit = 227 * 1024;
+// the sweep kernels' static shared memory (the dataflow queue slot) comes on top of the planned tile
+const int kSweepStatic = 128;
 // per-block shared memory that still lets two blocks share an SM (228 KB per
 // SM, 1 KB reserved per block)
-const int kSmemTwoPerSm = (228 * 1024 - 2 * 1024) / 2;
+const int kSmemTwoPerSm = (228 * 1024 - 2 * 1024) / 2 - kSweepStatic;
 
 thread_local std::string g_last_error;
 
@@ -171,7 +181,7 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
     // barriers then overlap the other's work: measured faster at 256^3);
     // pass 1 takes the largest shape that fits one block per SM.
     for (int pass = 0; pass < 2; pass++) {
-        const int limit = pass == 0 ? kSmemTwoPerSm : kSmemLimit;
+        const int limit = pass == 0 ? kSmemTwoPerSm : kSmemLimit - kSweepStatic;
         for (const Cand &c : all) {
             SnTile t;
             memset(&t, 0, sizeof(t));
@@ -294,6 +304,14 @@ struct sn_handle {
     SnWork *d_work = nullptr;
     std::vector<int> work_off, work_cnt, work_smem, work_thr;  // [phase*2 + variant]
     std::vector<int> fwork_off, fwork_cnt;           // per replica, all blocks
+    // dataflow sweep (one persistent launch per kernel variant and sweep)
+    bool flow = true;
+    int flow_items[2] = {0, 0}, flow_off[2] = {0, 0}, flow_grid[2] = {0, 0};
+    int *d_deps = nullptr;
+    uint32_t *d_done = nullptr;
+    size_t done_n = 0;
+    uint32_t *d_queue = nullptr;  // 2 counters
+    int *d_err = nullptr;
     std::vector<float *> lattice_mem;
     // scratch (lazy)
     float *d_stage = nullptr;
@@ -304,6 +322,10 @@ struct sn_handle {
     size_t grad_n = 0;
     double *d_trace = nullptr;
     size_t trace_n = 0;
+    SnAnalysisOffset *d_aoff = nullptr;  // analysis stencil table
+    size_t aoff_n = 0;
+    double *d_abins = nullptr;  // analysis reductions
+    size_t abins_n = 0;
     // graph
     cudaGraphExec_t graph = nullptr;
     uint64_t graph_nodes = 0;
@@ -396,25 +418,60 @@ sn_status recompute_one(sn_handle *h, int r, int prec, int record)
 
 // Issue one sweep's kernels on the handle's stream.  With events (2 per
 // launch), each block-colour launch is bracketed for timing.
+SnPhaseArgs phase_args(const sn_handle *h, int off, int cnt)
+{
+    SnPhaseArgs a;
+    a.work = h->d_work + off;
+    a.n_work = cnt;
+    a.reps = h->d_reps;
+    a.geoms = h->d_geoms;
+    a.acc = h->d_acc;
+    a.sweep = h->d_sweep;
+    a.cage = (float)h->params.cage_strain;
+    a.K = (float)h->params.K;
+    a.constrain = h->params.constrain_to_x;
+    a.dim = h->params.dim;
+    return a;
+}
+
 cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> *events)
 {
     cudaError_t e = cudaSuccess;
     size_t ev = 0;
+    if (h->flow) {
+        for (int v = 0; v < 2 && e == cudaSuccess; v++) {
+            if (!h->flow_items[v]) continue;
+            SnFlowArgs f;
+            // the phase-ordered items of a variant are contiguous in d_work
+            f.base = phase_args(h, h->flow_off[v], h->flow_items[v]);
+            f.deps = h->d_deps + (size_t)h->flow_off[v] * SN_MAX_DEPS;
+            f.done = h->d_done + h->flow_off[v];
+            f.queue = h->d_queue + v;
+            f.err = h->d_err;
+            int thr = 0, smem = 0;
+            for (int p = 0; p < 8; p++) {
+                thr = std::max(thr, h->work_thr[p * 2 + v]);
+                smem = std::max(smem, h->work_smem[p * 2 + v]);
+            }
+            if (events && ev + 1 < events->size()) e = cudaEventRecord((*events)[ev++], h->stream);
+            if (e == cudaSuccess)
+                e = k_flow[h->rc](v == 1, h->mixed, f, std::min(h->flow_grid[v], h->flow_items[v]), thr, smem,
+                                  h->stream, nullptr);
+            if (events && ev < events->size() && e == cudaSuccess) e = cudaEventRecord((*events)[ev++], h->stream);
+            if (nodes) (*nodes)++;
+        }
+        if (e == cudaSuccess) {
+            e = sn_launch_sweep_end(h->d_acc, h->d_state, h->d_hist, h->d_reps, h->nrep, h->d_sweep, h->d_ex,
+                                    h->d_order, h->d_queue, h->stream);
+            if (nodes) (*nodes)++;
+        }
+        return e;
+    }
     for (int p = 0; p < 8 && e == cudaSuccess; p++)
         for (int v = 0; v < 2 && e == cudaSuccess; v++) {
             const int k = p * 2 + v;
             if (!h->work_cnt[k]) continue;
-            SnPhaseArgs a;
-            a.work = h->d_work + h->work_off[k];
-            a.n_work = h->work_cnt[k];
-            a.reps = h->d_reps;
-            a.geoms = h->d_geoms;
-            a.acc = h->d_acc;
-            a.sweep = h->d_sweep;
-            a.cage = (float)h->params.cage_strain;
-            a.K = (float)h->params.K;
-            a.constrain = h->params.constrain_to_x;
-            a.dim = h->params.dim;
+            const SnPhaseArgs a = phase_args(h, h->work_off[k], h->work_cnt[k]);
             if (events && ev + 1 < events->size()) e = cudaEventRecord((*events)[ev++], h->stream);
             if (e == cudaSuccess) e = k_sweep[h->rc](v == 1, h->mixed, a, h->work_cnt[k], h->work_thr[k], h->work_smem[k], h->stream);
             if (events && ev < events->size() && e == cudaSuccess) e = cudaEventRecord((*events)[ev++], h->stream);
@@ -422,16 +479,39 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
         }
     if (e == cudaSuccess) {
         e = sn_launch_sweep_end(h->d_acc, h->d_state, h->d_hist, h->d_reps, h->nrep, h->d_sweep, h->d_ex, h->d_order,
-                                h->stream);
+                                nullptr, h->stream);
         if (nodes) (*nodes)++;
     }
     return e;
 }
 
+// Reads (and clears) the dataflow kernel's wait-timeout flag; the stream must be idle or is synchronised here.
+sn_status flow_status(sn_handle *h)
+{
+    if (!h->flow || !h->d_err) return SN_OK;
+    int err = 0;
+    SN_CK(h, cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if (!err) return SN_OK;
+    SN_CK(h, cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    return fail(h, SN_ERR_TIMEOUT, "a sweep block waited too long for its neighbours (dataflow schedule)");
+}
+
 sn_status capture_graph(sn_handle *h)
 {
-    // configure function attributes outside the capture
-    for (int v = 0; v < 2; v++) SN_CK(h, k_sweep[h->rc](v == 1, h->mixed, SnPhaseArgs{}, 0, 0, 0, h->stream));
+    // configure function attributes (and size the dataflow grid) outside the capture
+    for (int v = 0; v < 2; v++) {
+        SN_CK(h, k_sweep[h->rc](v == 1, h->mixed, SnPhaseArgs{}, 0, 0, 0, h->stream));
+        if (h->flow && h->flow_items[v]) {
+            int thr = 0, smem = 0;
+            for (int p = 0; p < 8; p++) {
+                thr = std::max(thr, h->work_thr[p * 2 + v]);
+                smem = std::max(smem, h->work_smem[p * 2 + v]);
+            }
+            SN_CK(h, k_flow[h->rc](v == 1, h->mixed, SnFlowArgs{}, 0, thr, smem, h->stream, &h->flow_grid[v]));
+            if (h->flow_grid[v] < 1) return fail(h, SN_ERR_CUDA, "dataflow kernel cannot be resident");
+        }
+    }
     cudaGraph_t g;
     SN_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     uint64_t nodes = 0;
@@ -452,8 +532,10 @@ void destroy_all(sn_handle *h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     for (float *p : h->lattice_mem) cudaFree(p);
-    void *ptrs[] = {h->d_reps, h->d_geoms, h->d_acc, h->d_state, h->d_sweep, h->d_hist, h->d_red, h->d_drift,
-                    h->d_ex,   h->d_order, h->d_flags, h->d_work, h->d_stage, h->d_site, h->d_grad, h->d_trace};
+    void *ptrs[] = {h->d_reps,  h->d_geoms, h->d_acc,   h->d_state, h->d_sweep, h->d_hist, h->d_red,
+                    h->d_drift, h->d_ex,    h->d_order, h->d_flags, h->d_work,  h->d_stage, h->d_site,
+                    h->d_grad,  h->d_trace, h->d_deps,  h->d_done,  h->d_queue, h->d_err,
+                    h->d_aoff,  h->d_abins};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -671,6 +753,57 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         h->fwork_cnt[r] = (int)work.size() - h->fwork_off[r];
     }
 
+    // dataflow lists: per kernel variant, the blocks in block-colour order, each with the indices of the
+    // adjacent blocks of earlier colour (the blocks whose sites its halo reads and that must finish first).
+    // Items only wait on items earlier in their list, which a running block has already taken.
+    std::vector<int> deps;
+    if (const char *env = getenv("SN_SCHEDULE")) h->flow = strcmp(env, "phases") != 0;
+    for (int v = 0; v < 2 && h->flow; v++) {
+        h->flow_off[v] = (int)work.size();
+        std::unordered_map<uint64_t, int> index;  // (replica, block) -> position in this list
+        for (int p = 0; p < 8; p++) {
+            const int k = p * 2 + v;
+            for (int i = 0; i < h->work_cnt[k]; i++) {
+                const SnWork w = work[h->work_off[k] + i];
+                const SnTile &t = h->tiles[w.rep];
+                const uint64_t key = (((uint64_t)w.rep * t.nb[0] + w.x0 / t.B[0]) * t.nb[1] + w.y0 / t.B[1]) *
+                                         t.nb[2] + w.z0 / t.B[2];
+                index[key] = (int)work.size() - h->flow_off[v];
+                work.push_back(w);
+            }
+        }
+        h->flow_items[v] = (int)work.size() - h->flow_off[v];
+        deps.resize((size_t)(h->flow_off[v] + h->flow_items[v]) * SN_MAX_DEPS, 0);
+        for (int i = 0; i < h->flow_items[v]; i++) {
+            const SnWork w = work[h->flow_off[v] + i];
+            const SnTile &t = h->tiles[w.rep];
+            const int b[3] = {w.x0 / t.B[0], w.y0 / t.B[1], w.z0 / t.B[2]};
+            auto colour = [&](const int *c) {
+                return (c[0] % t.m[0]) * 4 + (c[1] % t.m[1]) * 2 + (c[2] % t.m[2]);
+            };
+            const int own = colour(b);
+            int *dl = &deps[(size_t)(h->flow_off[v] + i) * SN_MAX_DEPS];
+            for (int dx = -1; dx <= 1; dx++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dz = -1; dz <= 1; dz++) {
+                        const int c[3] = {(b[0] + dx + t.nb[0]) % t.nb[0], (b[1] + dy + t.nb[1]) % t.nb[1],
+                                          (b[2] + dz + t.nb[2]) % t.nb[2]};
+                        if (c[0] == b[0] && c[1] == b[1] && c[2] == b[2]) continue;
+                        const int q = colour(c);
+                        if (q == own) return bail(fail(h, SN_ERR_SCHEDULE, "adjacent blocks share a colour"));
+                        if (q > own) continue;
+                        const uint64_t key = (((uint64_t)w.rep * t.nb[0] + c[0]) * t.nb[1] + c[1]) * t.nb[2] + c[2];
+                        const int j = index.at(key);
+                        bool seen = false;
+                        for (int u = 1; u <= dl[0]; u++) seen |= dl[u] == j;
+                        if (seen) continue;
+                        if (dl[0] + 1 >= SN_MAX_DEPS) return bail(fail(h, SN_ERR_SCHEDULE, "too many dependencies"));
+                        dl[++dl[0]] = j;
+                    }
+        }
+    }
+    if (h->flow) deps.resize(work.size() * SN_MAX_DEPS, 0);
+
     // temperature ladder for exchange: replicas sorted by T
     std::vector<int> order(n_replicas);
     for (int r = 0; r < n_replicas; r++) order[r] = r;
@@ -693,6 +826,13 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     ALLOC(h->d_order, nr * sizeof(int));
     ALLOC(h->d_flags, 4 * sizeof(int));
     ALLOC(h->d_work, std::max<size_t>(work.size(), 1) * sizeof(SnWork));
+    if (h->flow) {
+        ALLOC(h->d_deps, deps.size() * sizeof(int));
+        ALLOC(h->d_done, work.size() * sizeof(uint32_t));
+        h->done_n = work.size();
+        ALLOC(h->d_queue, 2 * sizeof(uint32_t));
+        ALLOC(h->d_err, sizeof(int));
+    }
 #undef ALLOC
     SnExchange ex;
     memset(&ex, 0, sizeof(ex));
@@ -703,6 +843,8 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_geoms, h->tiles.data(), nr * sizeof(SnTile), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_work, work.data(), work.size() * sizeof(SnWork), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_order, order.data(), nr * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && h->flow)
+        e = cudaMemcpyAsync(h->d_deps, deps.data(), deps.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_ex, &ex, sizeof(ex), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return bail(fail(h, SN_ERR_CUDA, "init upload: %s", cudaGetErrorString(e)));
@@ -794,7 +936,7 @@ sn_status sn_gpu_download_lattice(sn_handle *h, int replica, float *xyz, float *
     if (xyz) SN_CK(h, cudaMemcpyAsync(xyz, h->d_stage, 3 * N * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
     if (len) SN_CK(h, cudaMemcpyAsync(len, h->d_stage + 3 * N, N * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
     SN_CK(h, cudaStreamSynchronize(h->stream));
-    return SN_OK;
+    return flow_status(h);
 }
 
 sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *reject)
@@ -830,6 +972,8 @@ sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *r
         }
         if (accept) *accept = a;
         if (reject) *reject = t - a;
+        sn_status s = flow_status(h);
+        if (s) return s;
     }
     SN_CK(h, cudaGetLastError());
     return SN_OK;
@@ -839,6 +983,18 @@ sn_status sn_gpu_sweep_count(const sn_handle *h, uint64_t *sweeps)
 {
     if (!h || !sweeps) return fail(nullptr, SN_ERR_ARG, "null argument");
     *sweeps = h->sweeps;
+    return SN_OK;
+}
+
+sn_status sn_gpu_set_sweep_count(sn_handle *h, uint64_t sweeps)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    const uint32_t s32 = (uint32_t)sweeps;  // the device counter keys the random stream modulo 2^32
+    SN_CK(h, cudaMemcpyAsync(h->d_sweep, &s32, sizeof(s32), cudaMemcpyHostToDevice, h->stream));
+    // the dataflow done flags hold epochs of the old counter
+    if (h->d_done) SN_CK(h, cudaMemsetAsync(h->d_done, 0, h->done_n * sizeof(uint32_t), h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    h->sweeps = sweeps;
     return SN_OK;
 }
 
@@ -870,6 +1026,8 @@ sn_status sn_gpu_observables(sn_handle *h, double *E_per_site, double *P_abs, do
     std::vector<SnState> st(h->nrep);
     SN_CK(h, cudaMemcpyAsync(st.data(), h->d_state, h->nrep * sizeof(SnState), cudaMemcpyDeviceToHost, h->stream));
     SN_CK(h, cudaStreamSynchronize(h->stream));
+    sn_status fs = flow_status(h);
+    if (fs) return fs;
     for (int r = 0; r < h->nrep; r++) {
         const double N = (double)h->reps[r].n_sites;
         if (E_per_site) E_per_site[r] = st[r].E / N;
@@ -1093,7 +1251,10 @@ sn_status sn_gpu_phase_times(sn_handle *h, int n_sweeps, double *avg_launch_ms, 
 {
     if (!h || n_sweeps < 1) return fail(h, SN_ERR_ARG, "need a handle and n_sweeps >= 1");
     int nl = 0;
-    for (int k = 0; k < 16; k++) nl += h->work_cnt[k] ? 1 : 0;
+    if (h->flow)
+        for (int v = 0; v < 2; v++) nl += h->flow_items[v] ? 1 : 0;
+    else
+        for (int k = 0; k < 16; k++) nl += h->work_cnt[k] ? 1 : 0;
     std::vector<cudaEvent_t> ev(2 * (size_t)nl);
     for (auto &x : ev) SN_CK(h, cudaEventCreate(&x));
     cudaEvent_t s0, s1;
@@ -1121,6 +1282,8 @@ sn_status sn_gpu_phase_times(sn_handle *h, int n_sweeps, double *avg_launch_ms, 
     cudaEventDestroy(s0);
     cudaEventDestroy(s1);
     if (e != cudaSuccess) return fail(h, SN_ERR_CUDA, "phase timing: %s", cudaGetErrorString(e));
+    sn_status s = flow_status(h);
+    if (s) return s;
     if (avg_launch_ms) *avg_launch_ms = tot_launch / ((double)n_sweeps * nl);
     if (avg_sweep_ms) *avg_sweep_ms = tot_sweep / n_sweeps;
     if (launches_per_sweep) *launches_per_sweep = nl;
@@ -1196,6 +1359,209 @@ sn_status sn_gpu_proposals(const sn_handle *h, int replica, const uint32_t *site
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     cudaFree(d);
     if (e != cudaSuccess) return fail(const_cast<sn_handle *>(h), SN_ERR_CUDA, "proposal batch: %s", cudaGetErrorString(e));
+    return SN_OK;
+}
+
+}  // extern "C"
+
+// ---- analysis stencils: host tables and entry points ----
+namespace {
+
+// d = sqrt(float expression) stored to float, as the reference writes it
+// (src/starrynight-analysis.c:82,337,419,564).
+float ref_distance(float s) { return (float)std::sqrt((double)s); }
+
+SnAnalysisOffset make_offset(int dx, int dy, int dz)
+{
+    SnAnalysisOffset o;
+    memset(&o, 0, sizeof(o));
+    o.dx = dx;
+    o.dy = dy;
+    o.dz = dz;
+    return o;
+}
+
+// dipole_potential (src/starrynight-analysis.c:65-94): the cube |d_i| <= C in
+// dx, dy, dz order, without the origin, kept when d <= C; a = r.
+std::vector<SnAnalysisOffset> potential_table(int C)
+{
+    std::vector<SnAnalysisOffset> t;
+    for (int dx = -C; dx <= C; dx++)
+        for (int dy = -C; dy <= C; dy++)
+            for (int dz = -C; dz <= C; dz++) {
+                if (dx == 0 && dy == 0 && dz == 0) continue;
+                const float rx = (float)dx, ry = (float)dy, rz = (float)dz;
+                const float d = ref_distance(rx * rx + ry * ry + rz * rz);
+                if (d > (float)C) continue;
+                SnAnalysisOffset o = make_offset(dx, dy, dz);
+                o.a[0] = rx;
+                o.a[1] = ry;
+                o.a[2] = rz;
+                o.d3 = d * d * d;
+                t.push_back(o);
+            }
+    return t;
+}
+
+// dipole_electricfield (:393-450; half = 0) and dipole_electricfieldoffset
+// (:310-380; half = 1, displacements dx + 1/2 for dx in [-C-1, C-1], origin
+// not excluded): a = n = r/d, b = 3 n, kept when d <= C.
+std::vector<SnAnalysisOffset> efield_table(int C, bool half)
+{
+    std::vector<SnAnalysisOffset> t;
+    const int lo = half ? -C - 1 : -C, hi = half ? C - 1 : C;
+    for (int dx = lo; dx <= hi; dx++)
+        for (int dy = lo; dy <= hi; dy++)
+            for (int dz = lo; dz <= hi; dz++) {
+                if (!half && dx == 0 && dy == 0 && dz == 0) continue;
+                const float rx = half ? (float)((double)(float)dx + 0.5) : (float)dx;
+                const float ry = half ? (float)((double)(float)dy + 0.5) : (float)dy;
+                const float rz = half ? (float)((double)(float)dz + 0.5) : (float)dz;
+                const float d = ref_distance(rx * rx + ry * ry + rz * rz);
+                if (d > (float)C) continue;
+                SnAnalysisOffset o = make_offset(dx, dy, dz);
+                o.a[0] = rx / d;
+                o.a[1] = ry / d;
+                o.a[2] = rz / d;
+                for (int c = 0; c < 3; c++) o.b[c] = 3.0f * o.a[c];
+                o.d3 = d * d * d;
+                t.push_back(o);
+            }
+    return t;
+}
+
+// radial_order_parameter (:528-598): the ball |r|^2 <= C^2 including the
+// origin, binned by |r|^2; a = n = r/d with d = 1 at the origin.  Sorted by
+// bin, the reference's dx, dy, dz order kept within a bin.
+std::vector<SnAnalysisOffset> radial_table(int C)
+{
+    std::vector<SnAnalysisOffset> t;
+    for (int dx = -C; dx <= C; dx++)
+        for (int dy = -C; dy <= C; dy++)
+            for (int dz = -C; dz <= C; dz++) {
+                const int ds = dx * dx + dy * dy + dz * dz;
+                if (ds > C * C) continue;
+                float d = ref_distance((float)dx * dx + dy * dy + dz * dz);
+                if (d == 0) d = 1;
+                SnAnalysisOffset o = make_offset(dx, dy, dz);
+                o.bin = ds;
+                o.a[0] = (float)dx / d;
+                o.a[1] = (float)dy / d;
+                o.a[2] = (float)dz / d;
+                t.push_back(o);
+            }
+    std::stable_sort(t.begin(), t.end(),
+                     [](const SnAnalysisOffset &a, const SnAnalysisOffset &b) { return a.bin < b.bin; });
+    return t;
+}
+
+SnLatticeView view_of(const SnReplicaDev &R)
+{
+    SnLatticeView L;
+    L.px = R.px;
+    L.py = R.py;
+    L.pz = R.pz;
+    L.len = R.len;
+    L.X = R.X;
+    L.Y = R.Y;
+    L.Z = R.Z;
+    L.n = R.n_sites;
+    return L;
+}
+
+sn_status upload_table(sn_handle *h, const std::vector<SnAnalysisOffset> &t)
+{
+    sn_status s = ensure(h, (void **)&h->d_aoff, &h->aoff_n, std::max<size_t>(t.size(), 1), sizeof(SnAnalysisOffset));
+    if (s) return s;
+    SN_CK(h, cudaMemcpyAsync(h->d_aoff, t.data(), t.size() * sizeof(SnAnalysisOffset), cudaMemcpyHostToDevice,
+                             h->stream));
+    return SN_OK;
+}
+
+const int kAnalysisMaxCutoff = 32;
+
+}  // namespace
+
+extern "C" {
+
+sn_status sn_gpu_potential(sn_handle *h, int replica, int cutoff, double *pot)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (!pot || cutoff < 1 || cutoff > kAnalysisMaxCutoff)
+        return fail(h, SN_ERR_ARG, "potential: need an output buffer and 1 <= cutoff <= %d", kAnalysisMaxCutoff);
+    const SnReplicaDev &R = h->reps[replica];
+    const std::vector<SnAnalysisOffset> t = potential_table(cutoff);
+    if ((s = upload_table(h, t))) return s;
+    if ((s = ensure(h, (void **)&h->d_site, &h->site_n, (size_t)R.n_sites, sizeof(double)))) return s;
+    SN_CK(h, sn_launch_potential(view_of(R), h->d_aoff, (int)t.size(), h->d_site, h->stream));
+    SN_CK(h, cudaMemcpyAsync(pot, h->d_site, (size_t)R.n_sites * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_efield(sn_handle *h, int replica, int cutoff, int half_offset, double *magnitude)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (!magnitude || cutoff < 1 || cutoff > kAnalysisMaxCutoff)
+        return fail(h, SN_ERR_ARG, "efield: need an output buffer and 1 <= cutoff <= %d", kAnalysisMaxCutoff);
+    const SnReplicaDev &R = h->reps[replica];
+    const std::vector<SnAnalysisOffset> t = efield_table(cutoff, half_offset != 0);
+    if ((s = upload_table(h, t))) return s;
+    if ((s = ensure(h, (void **)&h->d_site, &h->site_n, (size_t)R.n_sites, sizeof(double)))) return s;
+    SN_CK(h, sn_launch_efield(view_of(R), h->d_aoff, (int)t.size(), half_offset ? 0 : 1, h->d_site, h->stream));
+    SN_CK(h, cudaMemcpyAsync(magnitude, h->d_site, (size_t)R.n_sites * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_radial_order(sn_handle *h, int replica, int cutoff, double *fe_sum, double *afe_sum,
+                              int64_t *count)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (cutoff < 1 || cutoff > kAnalysisMaxCutoff)
+        return fail(h, SN_ERR_ARG, "radial order: 1 <= cutoff <= %d", kAnalysisMaxCutoff);
+    const SnReplicaDev &R = h->reps[replica];
+    const int n_bins = cutoff * cutoff + 1;
+    const std::vector<SnAnalysisOffset> t = radial_table(cutoff);
+    if (count) {
+        for (int b = 0; b < n_bins; b++) count[b] = 0;
+        for (const SnAnalysisOffset &o : t) count[o.bin] += R.n_sites;
+    }
+    if ((s = upload_table(h, t))) return s;
+    if ((s = ensure(h, (void **)&h->d_abins, &h->abins_n, 2 * (size_t)n_bins, sizeof(double)))) return s;
+    SN_CK(h, cudaMemsetAsync(h->d_abins, 0, 2 * (size_t)n_bins * sizeof(double), h->stream));
+    SN_CK(h, sn_launch_radial(view_of(R), h->d_aoff, (int)t.size(), n_bins, h->d_abins, h->d_abins + n_bins,
+                              h->stream));
+    std::vector<double> out(2 * (size_t)n_bins);
+    SN_CK(h, cudaMemcpyAsync(out.data(), h->d_abins, out.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    for (int b = 0; b < n_bins; b++) {
+        if (fe_sum) fe_sum[b] = out[b];
+        if (afe_sum) afe_sum[b] = out[n_bins + b];
+    }
+    return SN_OK;
+}
+
+sn_status sn_gpu_order_parameters(sn_handle *h, int replica, double *polarisation_x, double *landau,
+                                  double *orientation_sum)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    const SnReplicaDev &R = h->reps[replica];
+    if ((s = ensure(h, (void **)&h->d_abins, &h->abins_n, 3, sizeof(double)))) return s;
+    SN_CK(h, cudaMemsetAsync(h->d_abins, 0, 3 * sizeof(double), h->stream));
+    SN_CK(h, sn_launch_orient_sum(view_of(R), h->d_abins, h->stream));
+    double o[3];
+    SN_CK(h, cudaMemcpyAsync(o, h->d_abins, sizeof(o), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if (polarisation_x) *polarisation_x = o[0] / (double)R.n_sites;
+    if (landau) *landau = o[0] * o[0] + o[1] * o[1] + o[2] * o[2];
+    if (orientation_sum)
+        for (int c = 0; c < 3; c++) orientation_sum[c] = o[c];
     return SN_OK;
 }
 

@@ -85,6 +85,21 @@ struct SnPhaseArgs {
     int dim;
 };
 
+#define SN_MAX_DEPS 28            // 1 count + up to 26 adjacent blocks (+1 spare)
+#define SN_WAIT_LIMIT (1 << 22)   // polls of a dependency flag before SN_ERR_TIMEOUT
+
+// Dataflow sweep: the work list holds every block of a kernel variant in
+// block-colour order; deps[item*SN_MAX_DEPS] = count, then the items of the
+// adjacent blocks with an earlier colour; done[item] = last sweep (epoch)
+// that finished the block; queue = next item to take (reset every sweep).
+struct SnFlowArgs {
+    SnPhaseArgs base;
+    const int *deps;
+    uint32_t *done;
+    uint32_t *queue;
+    int *err;
+};
+
 // Neighbour offset table for the per-site kernels (energy, adjoint, quench).
 struct SnNeighbour {
     int dx, dy, dz, unit;

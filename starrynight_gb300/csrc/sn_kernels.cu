@@ -87,8 +87,9 @@ __global__ void download_convert_kernel(const float *__restrict__ px, const floa
 // totals, log E/site and |P|/site, advance the sweep counter and, when due,
 // run one round of replica exchange between adjacent temperatures.
 __global__ void sweep_end_kernel(SnAccum *acc, SnState *state, double *hist, SnReplicaDev *reps, int nrep,
-                                 uint32_t *sweep, SnExchange *ex, int *order)
+                                 uint32_t *sweep, SnExchange *ex, int *order, uint32_t *queues)
 {
+    if (queues && threadIdx.x < 2) queues[threadIdx.x] = 0u;  // dataflow queues of the next sweep
     for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
         SnState &s = state[r];
         SnAccum &A = acc[r];
@@ -252,9 +253,9 @@ cudaError_t sn_launch_download_convert(const float *px, const float *py, const f
 }
 
 cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnReplicaDev *reps, int nrep,
-                                uint32_t *sweep, SnExchange *ex, int *order, cudaStream_t st)
+                                uint32_t *sweep, SnExchange *ex, int *order, uint32_t *queues, cudaStream_t st)
 {
-    sweep_end_kernel<<<1, 256, 0, st>>>(acc, state, hist, reps, nrep, sweep, ex, order);
+    sweep_end_kernel<<<1, 256, 0, st>>>(acc, state, hist, reps, nrep, sweep, ex, order, queues);
     return cudaGetLastError();
 }
 

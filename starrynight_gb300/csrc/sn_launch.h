@@ -18,9 +18,12 @@ typedef cudaError_t (*sn_sweep_launch_fn)(bool two_d, bool mixed, const SnPhaseA
 typedef cudaError_t (*sn_field_launch_fn)(bool fp64, bool two_d, bool mixed, const void *field_args, int grid,
                                           int threads, int smem, cudaStream_t st);
 typedef void (*sn_geo_fn)(bool two_d, int *S, int *SZ, int *NS, int *NF, int *merge);
+typedef cudaError_t (*sn_flow_launch_fn)(bool two_d, bool mixed, const SnFlowArgs &a, int grid, int threads, int smem,
+                                         cudaStream_t st, int *max_grid);
 
 #define SN_DECLARE_RC(N)                                                                                     \
     cudaError_t sn_launch_sweep_rc##N(bool, bool, const SnPhaseArgs &, int, int, int, cudaStream_t);        \
+    cudaError_t sn_launch_flow_rc##N(bool, bool, const SnFlowArgs &, int, int, int, cudaStream_t, int *);   \
     cudaError_t sn_launch_field_rc##N(bool, bool, bool, const void *, int, int, int, cudaStream_t);        \
     void sn_geo_rc##N(bool, int *, int *, int *, int *, int *);
 SN_DECLARE_RC(1)
@@ -77,7 +80,7 @@ cudaError_t sn_launch_upload_convert(const float *stage_xyz, const float *stage_
 cudaError_t sn_launch_download_convert(const float *px, const float *py, const float *pz, const float *len,
                                        float *stage_xyz, float *stage_len, long long n, cudaStream_t st);
 cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnReplicaDev *reps, int nrep,
-                                uint32_t *sweep, SnExchange *ex, int *order, cudaStream_t st);
+                                uint32_t *sweep, SnExchange *ex, int *order, uint32_t *queues, cudaStream_t st);
 cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
                                        double cage, double *drift_max, int record, cudaStream_t st);
 cudaError_t sn_launch_quench_step(float *px, float *py, float *pz, const float *len, const float *grad,
@@ -86,3 +89,31 @@ cudaError_t sn_launch_fma_peak(float *out, int blocks, int threads, int iters, c
 cudaError_t sn_launch_philox_batch(const uint32_t *ctr, const uint32_t *key, uint32_t *out, int n, cudaStream_t st);
 cudaError_t sn_launch_proposal_batch(const uint32_t *site, uint32_t sweep, uint32_t seed_lo, uint32_t seed_hi,
                                      int dim, int constrain, float *out4, int n, cudaStream_t st);
+
+// ---- analysis stencils (sn_analysis.cu) ----
+
+// One replica's lattice arrays (z fastest) as the analysis kernels read them.
+struct SnLatticeView {
+    const float *px, *py, *pz, *len;
+    int X, Y, Z;
+    long long n;
+};
+
+// One displacement of an analysis stencil, with the per-offset constants the
+// reference computes on the fly: a = r (potential) or r/d (field, correlation),
+// b = 3 r/d (field), d3 = d*d*d in float, bin = |r|^2 (correlation).
+struct SnAnalysisOffset {
+    int dx, dy, dz, bin;
+    float a[3];
+    float d3;
+    float b[3];
+    float pad;
+};
+
+cudaError_t sn_launch_potential(const SnLatticeView &L, const SnAnalysisOffset *off, int n_off, double *out,
+                                cudaStream_t st);
+cudaError_t sn_launch_efield(const SnLatticeView &L, const SnAnalysisOffset *off, int n_off, int self_term,
+                             double *out, cudaStream_t st);
+cudaError_t sn_launch_radial(const SnLatticeView &L, const SnAnalysisOffset *off, int n_off, int n_bins,
+                             double *fe, double *afe, cudaStream_t st);
+cudaError_t sn_launch_orient_sum(const SnLatticeView &L, double *out3, cudaStream_t st);

@@ -258,8 +258,11 @@ __device__ __forceinline__ void build_tables(const SnTile &Gm, int *start, int *
     }
 }
 
-// Asynchronous copy of block + halo (periodic wrap) into the class-major tile.
-template <int RC, bool TWO_D, bool MIXED>
+// Copy of block + halo (periodic wrap) into the class-major tile.  Phase
+// launches use asynchronous copies through L1 (L1 starts clean at every
+// launch).  The dataflow kernel reads blocks other SMs wrote during the same
+// launch, and L1 is not coherent across SMs, so COHERENT loads go to L2.
+template <int RC, bool TWO_D, bool MIXED, bool COHERENT = false>
 __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, float *tile,
                                            float *tlen, const int *start, int tid, int nthreads)
 {
@@ -277,10 +280,18 @@ __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &
             const int gz = TWO_D ? 0 : sn_wrap(w.z0 - HZ + uz, Z);
             const long long g = gb + gz;
             const int slot = rslot + uz;  // z is stored plainly
-            cp_async4(&tile[3 * slot + 0], R.px + g);
-            cp_async4(&tile[3 * slot + 1], R.py + g);
-            cp_async4(&tile[3 * slot + 2], R.pz + g);
-            if constexpr (MIXED) cp_async4(&tlen[slot], R.len + g);
+            if constexpr (COHERENT) {
+                const float x = __ldcg(R.px + g), y = __ldcg(R.py + g), z = __ldcg(R.pz + g);
+                tile[3 * slot + 0] = x;
+                tile[3 * slot + 1] = y;
+                tile[3 * slot + 2] = z;
+                if constexpr (MIXED) tlen[slot] = __ldg(R.len + g);  // lengths never change in a sweep
+            } else {
+                cp_async4(&tile[3 * slot + 0], R.px + g);
+                cp_async4(&tile[3 * slot + 1], R.py + g);
+                cp_async4(&tile[3 * slot + 2], R.pz + g);
+                if constexpr (MIXED) cp_async4(&tlen[slot], R.len + g);
+            }
         }
     }
 }
@@ -290,17 +301,15 @@ __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &
 // tt = tid % tg of every colour group: half h = tt / tp of the group, target
 // t = tt % tp = (qx, qy, qz) of that colour (inactive where the colour has
 // fewer targets).  Threads with j == 0 also finalize their target.
-template <int RC, bool TWO_D, bool MIXED>
-__global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseArgs a)
+template <int RC, bool TWO_D, bool MIXED, bool FLOW>
+__device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a, unsigned char *smem)
 {
     using G = Geo<RC, TWO_D>;
     constexpr int S = G::S, H = G::H, HZ = G::HZ, SZ = G::SZ, NF = G::NF, NS = G::NS;
     constexpr bool MERGE = G::MERGE;
-    extern __shared__ __align__(16) unsigned char smem[];
 
     const int tid = threadIdx.x, nthreads = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5;
-    const SnWork w = a.work[blockIdx.x];
     const SnReplicaDev &R = a.reps[w.rep];
     const SnTile &Gm = a.geoms[R.geom];
 
@@ -330,7 +339,7 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseAr
     double *red = reinterpret_cast<double *>(smem + cv.red);
 
     build_tables<RC, TWO_D>(Gm, start, ftab, tid, nthreads);
-    stage_tile<RC, TWO_D, MIXED>(R, Gm, w, tile, tlen, start, tid, nthreads);
+    stage_tile<RC, TWO_D, MIXED, FLOW>(R, Gm, w, tile, tlen, start, tid, nthreads);
 
     // this thread's fixed role
     const int j = tid / tg, tt = tid - (tid / tg) * tg;
@@ -377,7 +386,9 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseAr
                             float3 p;
                             float u;
                             if (!sn_proposal((uint32_t)site, sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
-                                p = make_float3(gpx[site], gpy[site], gpz[site]);
+                                p = make_float3(FLOW ? __ldcg(gpx + site) : gpx[site],
+                                                FLOW ? __ldcg(gpy + site) : gpy[site],
+                                                FLOW ? __ldcg(gpz + site) : gpz[site]);
                             // accept iff dE < -ln(u)/beta  <=>  dE < 0 || exp(-beta dE) > u
                             const float thr = u > 0.0f ? -logf(u) / beta : INFINITY;
                             pr = make_float4(p.x, p.y, p.z, thr);
@@ -476,6 +487,70 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseAr
         else if (tid < 4) atomicAdd(&A->dP[tid - 1], s);
         else if (tid == 4) atomicAdd(&A->acc, (unsigned long long)s);
         else atomicAdd(&A->att, (unsigned long long)s);
+    }
+}
+
+// One block colour per launch, one CTA per block.
+template <int RC, bool TWO_D, bool MIXED>
+__global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    sweep_block<RC, TWO_D, MIXED, false>(a.work[blockIdx.x], a, smem);
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(uint32_t *p, uint32_t v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Dataflow sweep: one persistent launch per sweep.  Every CTA is resident
+// (the host sizes the grid with the occupancy API) and takes blocks from a
+// queue ordered by block colour.  Before updating a block it waits until
+// each adjacent block of an earlier colour has finished this sweep (a
+// bounded spin; on time-out it records SN_ERR_TIMEOUT in *err and goes on).
+// Adjacent blocks of later colours wait for this one in turn, so every block
+// sees exactly the lattice the phase-by-phase order gives it.  Deadlock
+// cannot occur: a block waited on was taken from the queue earlier by a CTA
+// that is running, and it only waits on blocks taken before it.
+template <int RC, bool TWO_D, bool MIXED>
+__global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_flow(const SnFlowArgs f)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    const uint32_t epoch = *f.base.sweep + 1u;
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(f.queue, 1u);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= f.base.n_work) break;
+        const int *dl = f.deps + (size_t)item * SN_MAX_DEPS;
+        if (tid < dl[0]) {
+            const uint32_t *flag = f.done + dl[1 + tid];
+            for (int it = 0; ld_acquire_gpu(flag) < epoch; it++) {
+                if (it >= SN_WAIT_LIMIT) {
+                    atomicOr(f.err, 1);
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __syncthreads();
+        __threadfence();
+        sweep_block<RC, TWO_D, MIXED, true>(f.base.work[item], f.base, smem);
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            st_release_gpu(f.done + item, epoch);
+        }
     }
 }
 
@@ -681,6 +756,38 @@ cudaError_t launch_rc(bool two_d, bool mixed, const SnPhaseArgs &args, int grid,
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e != cudaSuccess) return e;
         configured[idx] = true;
+    }
+    if (grid <= 0) return cudaSuccess;
+    fn<<<grid, threads, smem_bytes, st>>>(args);
+    return cudaGetLastError();
+}
+
+template <int RC>
+cudaError_t launch_flow_rc(bool two_d, bool mixed, const SnFlowArgs &args, int grid, int threads, int smem_bytes,
+                           cudaStream_t st, int *max_grid)
+{
+    static bool configured[4] = {false, false, false, false};
+    const int idx = (two_d ? 2 : 0) + (mixed ? 1 : 0);
+    void (*fn)(const SnFlowArgs);
+    if (two_d) fn = mixed ? sweep_flow<RC, true, true> : sweep_flow<RC, true, false>;
+    else fn = mixed ? sweep_flow<RC, false, true> : sweep_flow<RC, false, false>;
+    if (!configured[idx]) {
+        // the queue slot is static shared memory: the dynamic limit is what remains of 227 KB
+        cudaFuncAttributes fa;
+        cudaError_t e = cudaFuncGetAttributes(&fa, fn);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     227 * 1024 - (int)fa.sharedSizeBytes);
+        if (e != cudaSuccess) return e;
+        configured[idx] = true;
+    }
+    if (max_grid) {
+        int per_sm = 0, dev = 0, nsm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem_bytes);
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        *max_grid = per_sm * nsm;
     }
     if (grid <= 0) return cudaSuccess;
     fn<<<grid, threads, smem_bytes, st>>>(args);

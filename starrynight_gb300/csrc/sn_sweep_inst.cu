@@ -27,6 +27,12 @@ cudaError_t SN_CAT(sn_launch_field_rc, SN_RC)(bool fp64, bool two_d, bool mixed,
     return sn_sweep::launch_field_rc<float, SN_RC>(two_d, mixed, fa, grid, threads, smem, st);
 }
 
+cudaError_t SN_CAT(sn_launch_flow_rc, SN_RC)(bool two_d, bool mixed, const SnFlowArgs &a, int grid, int threads,
+                                             int smem, cudaStream_t st, int *max_grid)
+{
+    return sn_sweep::launch_flow_rc<SN_RC>(two_d, mixed, a, grid, threads, smem, st, max_grid);
+}
+
 void SN_CAT(sn_geo_rc, SN_RC)(bool two_d, int *S, int *SZ, int *NS, int *NF, int *merge)
 {
     sn_sweep::geo_sizes<SN_RC>(two_d, *S, *SZ, *NS, *NF, *merge);

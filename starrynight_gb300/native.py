@@ -20,7 +20,7 @@ MAX_CUTOFF = 6
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
            "-I" + CSRC, "-I" + INCLUDE]
 
 
@@ -60,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             obj = os.path.join(LIBDIR, "sn_sweep_rc%d.o" % rc)
             jobs.append([NVCC] + ARCH + NVFLAGS + ["-DSN_RC=%d" % rc, "-c", os.path.join(CSRC, "sn_sweep_inst.cu"),
                                                    "-o", obj])
-        for name in ("sn_kernels", "sn_gpu", "sn_noalloc"):
+        for name in ("sn_kernels", "sn_gpu", "sn_noalloc", "sn_analysis"):
             jobs.append([NVCC] + ARCH + NVFLAGS + ["-c", os.path.join(CSRC, name + ".cu"),
                                                    "-o", os.path.join(LIBDIR, name + ".o")])
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
@@ -71,12 +71,30 @@ def build(force: bool = False, verbose: bool = False) -> str:
         tmp = so + ".tmp"
         _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
         os.replace(tmp, so)
+    io = build_io(force)
     drv = driver_path()
     dsrc = [os.path.join(PKG, "driver", "starrynight-gpu.c"), os.path.join(PKG, "cfg", "libconfig_min.c")]
-    if all(os.path.exists(p) for p in dsrc) and (force or _stale(drv, dsrc + [so])):
+    if all(os.path.exists(p) for p in dsrc) and (force or _stale(drv, dsrc + [so, io, os.path.join(INCLUDE, "sn_gpu.h")])):
         _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-I" + INCLUDE, "-I" + os.path.join(PKG, "cfg"), "-o", drv] + dsrc +
-             ["-L" + LIBDIR, "-lsn_gpu", "-Wl,-rpath,$ORIGIN", "-lm"])
+             ["-L" + LIBDIR, "-lsn_gpu", "-lsn_io", "-Wl,-rpath,$ORIGIN", "-lm"])
     return so
+
+
+def io_path() -> str:
+    return os.path.join(LIBDIR, "libsn_io.so")
+
+
+def build_io(force: bool = False) -> str:
+    """Host-only output-format and checkpoint library (no CUDA)."""
+    os.makedirs(LIBDIR, exist_ok=True)
+    io = io_path()
+    src = [os.path.join(PKG, "io", "sn_io.c"), os.path.join(INCLUDE, "sn_io.h")]
+    if force or _stale(io, src):
+        tmp = io + ".tmp"
+        _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-Wall", "-fPIC", "-shared", "-I" + INCLUDE, "-o", tmp,
+              src[0], "-lm"])
+        os.replace(tmp, io)
+    return io
 
 
 if __name__ == "__main__":

@@ -194,6 +194,36 @@ class Simulation:
         self._ck(lib().sn_gpu_sweep_count(self._h, ctypes.byref(v)))
         return v.value
 
+    def set_sweep_count(self, sweeps: int) -> None:
+        """Restore the sweep counter that keys the random stream (resume from a checkpoint)."""
+        self._ck(lib().sn_gpu_set_sweep_count(self._h, int(sweeps)))
+
+    # -- analysis (src/starrynight-analysis.c) ------------------------------------
+    def potential(self, replica: int = 0, cutoff: int = 6) -> np.ndarray:
+        """dipole_potential at every site (FP64, bit-equal to the reference)."""
+        out = np.zeros(self.n_sites(replica), np.float64)
+        self._ck(lib().sn_gpu_potential(self._h, replica, int(cutoff), _ptr(out)))
+        return out
+
+    def efield(self, replica: int = 0, cutoff: int = 4, half_offset: bool = False) -> np.ndarray:
+        """|E| of dipole_electricfield (or dipole_electricfieldoffset) at every site."""
+        out = np.zeros(self.n_sites(replica), np.float64)
+        self._ck(lib().sn_gpu_efield(self._h, replica, int(cutoff), int(bool(half_offset)), _ptr(out)))
+        return out
+
+    def radial_order(self, replica: int = 0, cutoff: int = 9):
+        """(fe_sum, afe_sum, count) per |r|^2 bin of radial_order_parameter (FP64 sums)."""
+        nb = cutoff * cutoff + 1
+        fe, afe, cnt = np.zeros(nb), np.zeros(nb), np.zeros(nb, np.int64)
+        self._ck(lib().sn_gpu_radial_order(self._h, replica, int(cutoff), _ptr(fe), _ptr(afe), _ptr(cnt)))
+        return fe, afe, cnt
+
+    def order_parameters(self, replica: int = 0):
+        """(polarisation() = sum p_x / N, landau_order() = |sum p|^2, sum p) -- unweighted."""
+        pol, lan, s3 = ctypes.c_double(0.0), ctypes.c_double(0.0), np.zeros(3)
+        self._ck(lib().sn_gpu_order_parameters(self._h, replica, ctypes.byref(pol), ctypes.byref(lan), _ptr(s3)))
+        return pol.value, lan.value, s3
+
     # -- energies / observables -----------------------------------------------------
     def energy(self, replica: int = 0, precision: str = "fp32", site: bool = False):
         prec = _abi.SN_ENERGY_FP64 if precision == "fp64" else _abi.SN_ENERGY_FP32

@@ -13,8 +13,17 @@ the reference itself are what pin the CPU oracle:
   ref_equilibrium.npz   per-sweep E/site and |P|/site of random-sequential runs
                         (statistical oracle): 32^3, cutoff 3, CageStrain 1,
                         T in {50,150,300,500}, 4 seeds each
+  ref_analysis.npz      dipole_potential, dipole_electricfield(4),
+                        dipole_electricfieldoffset(2) maps, polarisation(),
+                        landau_order() and the radial_order_parameter file for
+                        random, patterned, slab and mixed lattices
+  ref_files.npz         the bytes of every analysis writer on one 10^3 lattice
+                        with vacancies, plus the captured stderr of
+                        outputlattice_dumb_terminal and recombination_calculator
+  ref_driver_files.npz  the files the stock reference binary writes for a 10x12x14
+                        "spectrum" run with every analysis flag on and no moves
 
-Usage:  python tests/golden/make_golden.py [--skip-equilibrium]
+Usage:  python tests/golden/make_golden.py [--skip-equilibrium] [--analysis-only]
 """
 from __future__ import annotations
 
@@ -127,15 +136,129 @@ def equilibrium():
                         L=EQ_L, equil=EQ_EQUIL, prod=EQ_PROD)
 
 
+ANALYSIS_CASES = [
+    dict(name="random10", X=10, Y=10, Z=10, cutoff=3, T=300),
+    dict(name="spectrum", X=10, Y=12, Z=14, cutoff=3, T=150, pattern="spectrum"),
+    dict(name="buckled", X=10, Y=10, Z=10, cutoff=3, T=300, pattern="buckled"),
+    dict(name="slab12", X=12, Y=12, Z=1, cutoff=3, T=300),
+    dict(name="mixture10", X=10, Y=10, Z=10, cutoff=3, T=250, lengths=(1.0, 0.5, 0.0), prevalence=(0.5, 0.3, 0.2)),
+]
+
+
+def _zero_vacancies(r):
+    """Vacancies as zero vectors (the GPU build's convention) in the reference's own lattice."""
+    lat = r.lattice()
+    lat[lat[:, 3] == 0, :3] = 0.0
+    r.set_lattice(lat)
+    return lat
+
+
+def _parse_rdf(path):
+    rows = [l.split() for l in open(path) if l.strip() and not l.startswith("#")]
+    return np.array([[float(v) for v in row] for row in rows])
+
+
+def analysis(R, tmp):
+    out = {}
+    for c in ANALYSIS_CASES:
+        r = _sim(R, c)
+        if "pattern" in c:
+            r.init_pattern(c["pattern"])
+        n = c["name"]
+        out[n + "/lattice"] = _zero_vacancies(r)
+        out[n + "/shape"] = np.array([c["X"], c["Y"], c["Z"]])
+        out[n + "/potential"] = r.potential_map()
+        out[n + "/efield4"] = r.efield_map(4)
+        out[n + "/efieldoffset2"] = r.efield_map(2, half=True)
+        pol, landau = r.observables()
+        out[n + "/order"] = np.array([pol, landau])
+        path = os.path.join(tmp, n + "-rdf.dat")
+        r.write("rdf", path)
+        out[n + "/rdf"] = _parse_rdf(path)
+    np.savez_compressed(os.path.join(HERE, "ref_analysis.npz"), **out)
+
+
+WRITERS = ("potential_xyz", "potential_cube", "efield_xyz", "efieldoffset_xyz", "potential_pgm", "dipoles_xyz",
+           "dipoles_ppm", "dipoles_svg", "rdf", "recombination")
+
+
+def files(R, tmp):
+    c = dict(X=10, Y=10, Z=10, cutoff=3, T=300, lengths=(1.0, 0.0), prevalence=(0.8, 0.2))
+    r = _sim(R, c)
+    out = {"lattice": _zero_vacancies(r), "shape": np.array([10, 10, 10]), "T": np.array(300),
+           "potential": r.potential_map(), "efield4": r.efield_map(4), "efieldoffset2": r.efield_map(2, half=True)}
+    for kind in WRITERS:
+        path = os.path.join(tmp, "w_" + kind)
+        r.write(kind, path)
+        out["file/" + kind] = np.frombuffer(open(path, "rb").read(), np.uint8)
+    for kind in ("dumb_terminal", "recombination"):
+        path = os.path.join(tmp, "c_" + kind)
+        r.capture(kind, path)
+        out["stderr/" + kind] = np.frombuffer(open(path, "rb").read(), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "ref_files.npz"), **out)
+
+
+DRIVER_CFG = """T = 300
+X = 10
+Y = 12
+Z = 14
+InitialLattice = "spectrum"
+Efield: { x = 0.0; y = 0.0; z = 0.0; }
+DipoleCutOff = 3
+ConstrainToX = false
+K = 0.0
+Dipoles = [ 1.0 ];
+Prevalence = [ 1.0 ];
+CageStrain = 1.0
+MCMegaSteps = 0
+MCEqmSteps = 0
+MCMoves = 1.0
+DisplayDumbTerminal = false
+CalculateRecombination = false
+CalculateRadialOrderParameter = true
+CalculatePotential = true
+CalculateEfield = true
+SaveDipolesPNG = true
+SaveDipolesSVG = true
+SaveDipolesXYZ = true
+SavePotentialCube = true
+"""
+
+
+def driver_files(tmp):
+    """Run the stock reference binary (oracle/_ref/starrynight) in a scratch directory."""
+    import subprocess
+    exe = os.path.join(ROOT, "oracle", "_ref", "starrynight")
+    d = os.path.join(tmp, "driver")
+    os.makedirs(d, exist_ok=True)
+    with open(os.path.join(d, "starrynight.cfg"), "w") as f:
+        f.write(DRIVER_CFG)
+    subprocess.run([exe], cwd=d, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    out = {"cfg": np.frombuffer(DRIVER_CFG.encode(), np.uint8)}
+    for name in sorted(os.listdir(d)):
+        if name in ("starrynight.cfg",) or name.endswith(".log"):
+            continue
+        out["file/" + name] = np.frombuffer(open(os.path.join(d, name), "rb").read(), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "ref_driver_files.npz"), **out)
+
+
 def main():
     from oracle import oracle as O
     from oracle import ref_harness as R
     O.build(ref=True)
     if not R.available():
         raise SystemExit("the reference harness is not built (reference tree missing?)")
-    neighbours(R)
-    trajectories(R)
-    site_energies(R)
+    import tempfile
+    if "--analysis-only" not in sys.argv:
+        neighbours(R)
+        trajectories(R)
+        site_energies(R)
+    with tempfile.TemporaryDirectory() as tmp:
+        analysis(R, tmp)
+        files(R, tmp)
+        driver_files(tmp)
+    if "--analysis-only" in sys.argv:
+        return
     if "--skip-equilibrium" not in sys.argv:
         equilibrium()
 
