@@ -154,7 +154,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 def read_traffic():
     """DRAM bytes per launch of the sweep kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "sweep_phase_256cubed.md")
+    path = os.path.join(ROOT, "profiles", "sweep_flow_256cubed.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):

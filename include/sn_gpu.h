@@ -289,6 +289,12 @@ void *sn_gpu_stream(const sn_handle *h);
  * of the sweep kernel with CUDA events on the handle's stream:
  * *avg_launch_ms = mean duration of one launch, *avg_sweep_ms = mean sweep.
  * The sweeps are real (they advance the lattice and the sweep counter). */
+/* Dataflow schedule statistics since the last call: stats[0] = 1 when the
+ * sweep runs as one dataflow launch per kernel variant (0: one launch per
+ * block colour), stats[1] = its resident grid (3D variant), stats[2] = blocks
+ * that had to wait for a neighbour, stats[3] = polls spent waiting.
+ * Measurement hook; no reference counterpart. */
+sn_status sn_gpu_flow_stats(sn_handle *h, uint64_t *stats);
 sn_status sn_gpu_phase_times(sn_handle *h, int n_sweeps, double *avg_launch_ms, double *avg_sweep_ms,
                              int *launches_per_sweep);
 /* Measured FP32 FMA throughput of the current device (TFLOP/s, an FMA

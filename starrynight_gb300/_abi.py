@@ -111,6 +111,7 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_phase_times": ([h, _i, _P(ctypes.c_double), _P(ctypes.c_double), _P(_i)], _i),
             "sn_gpu_proposals": ([h, _i, _vp, _i, ctypes.c_uint32, _vp], _i),
             "sn_gpu_potential": ([h, _i, _i, _vp], _i),
+            "sn_gpu_flow_stats": ([h, _vp], _i),
             "sn_gpu_efield": ([h, _i, _i, _i, _vp], _i),
             "sn_gpu_radial_order": ([h, _i, _i, _vp, _vp, _vp], _i),
             "sn_gpu_order_parameters": ([h, _i, _P(ctypes.c_double), _P(ctypes.c_double), _vp], _i),

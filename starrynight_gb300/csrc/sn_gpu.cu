@@ -311,7 +311,8 @@ struct sn_handle {
     uint32_t *d_done = nullptr;
     size_t done_n = 0;
     uint32_t *d_queue = nullptr;  // 2 counters
-    int *d_err = nullptr;
+    uint32_t *d_err = nullptr;    // timeout flag, stall statistics
+    int flow_async = 1;
     std::vector<float *> lattice_mem;
     // scratch (lazy)
     float *d_stage = nullptr;
@@ -448,6 +449,7 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
             f.done = h->d_done + h->flow_off[v];
             f.queue = h->d_queue + v;
             f.err = h->d_err;
+            f.async_stage = h->flow_async;
             int thr = 0, smem = 0;
             for (int p = 0; p < 8; p++) {
                 thr = std::max(thr, h->work_thr[p * 2 + v]);
@@ -489,11 +491,11 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
 sn_status flow_status(sn_handle *h)
 {
     if (!h->flow || !h->d_err) return SN_OK;
-    int err = 0;
-    SN_CK(h, cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    uint32_t err = 0;
+    SN_CK(h, cudaMemcpyAsync(&err, h->d_err, sizeof(err), cudaMemcpyDeviceToHost, h->stream));
     SN_CK(h, cudaStreamSynchronize(h->stream));
     if (!err) return SN_OK;
-    SN_CK(h, cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    SN_CK(h, cudaMemsetAsync(h->d_err, 0, sizeof(err), h->stream));
     return fail(h, SN_ERR_TIMEOUT, "a sweep block waited too long for its neighbours (dataflow schedule)");
 }
 
@@ -758,6 +760,7 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     // Items only wait on items earlier in their list, which a running block has already taken.
     std::vector<int> deps;
     if (const char *env = getenv("SN_SCHEDULE")) h->flow = strcmp(env, "phases") != 0;
+    if (const char *env = getenv("SN_FLOW_STAGE")) h->flow_async = strcmp(env, "coherent") != 0;
     for (int v = 0; v < 2 && h->flow; v++) {
         h->flow_off[v] = (int)work.size();
         std::unordered_map<uint64_t, int> index;  // (replica, block) -> position in this list
@@ -831,7 +834,7 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         ALLOC(h->d_done, work.size() * sizeof(uint32_t));
         h->done_n = work.size();
         ALLOC(h->d_queue, 2 * sizeof(uint32_t));
-        ALLOC(h->d_err, sizeof(int));
+        ALLOC(h->d_err, 4 * sizeof(uint32_t));
     }
 #undef ALLOC
     SnExchange ex;
@@ -1287,6 +1290,22 @@ sn_status sn_gpu_phase_times(sn_handle *h, int n_sweeps, double *avg_launch_ms, 
     if (avg_launch_ms) *avg_launch_ms = tot_launch / ((double)n_sweeps * nl);
     if (avg_sweep_ms) *avg_sweep_ms = tot_sweep / n_sweeps;
     if (launches_per_sweep) *launches_per_sweep = nl;
+    return SN_OK;
+}
+
+sn_status sn_gpu_flow_stats(sn_handle *h, uint64_t *stats)
+{
+    if (!h || !stats) return fail(h, SN_ERR_ARG, "null argument");
+    uint32_t e[4] = {0, 0, 0, 0};
+    if (h->flow && h->d_err) {
+        SN_CK(h, cudaMemcpyAsync(e, h->d_err, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+        SN_CK(h, cudaMemsetAsync(h->d_err + 1, 0, 3 * sizeof(uint32_t), h->stream));
+        SN_CK(h, cudaStreamSynchronize(h->stream));
+    }
+    stats[0] = h->flow ? 1 : 0;
+    stats[1] = (uint64_t)(h->flow ? h->flow_grid[0] : 0);
+    stats[2] = e[1];
+    stats[3] = e[2];
     return SN_OK;
 }
 

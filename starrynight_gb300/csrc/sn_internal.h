@@ -97,7 +97,8 @@ struct SnFlowArgs {
     const int *deps;
     uint32_t *done;
     uint32_t *queue;
-    int *err;
+    uint32_t *err;    // [0] wait timed out, [1] items that waited, [2] polls
+    int async_stage;  // stage tiles with cp.async (1) or L1-bypassing loads (0)
 };
 
 // Neighbour offset table for the per-site kernels (energy, adjoint, quench).

@@ -258,10 +258,11 @@ __device__ __forceinline__ void build_tables(const SnTile &Gm, int *start, int *
     }
 }
 
-// Copy of block + halo (periodic wrap) into the class-major tile.  Phase
-// launches use asynchronous copies through L1 (L1 starts clean at every
-// launch).  The dataflow kernel reads blocks other SMs wrote during the same
-// launch, and L1 is not coherent across SMs, so COHERENT loads go to L2.
+// Copy of block + halo (periodic wrap) into the class-major tile, by
+// asynchronous copies through L1, or (COHERENT) by loads that bypass L1.  The
+// dataflow kernel reads blocks other SMs wrote during the same launch; its
+// acquire of their done flags followed by a gpu-scope fence orders those
+// writes before either kind of load.
 template <int RC, bool TWO_D, bool MIXED, bool COHERENT = false>
 __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, float *tile,
                                            float *tlen, const int *start, int tid, int nthreads)
@@ -301,7 +302,7 @@ __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &
 // tt = tid % tg of every colour group: half h = tt / tp of the group, target
 // t = tt % tp = (qx, qy, qz) of that colour (inactive where the colour has
 // fewer targets).  Threads with j == 0 also finalize their target.
-template <int RC, bool TWO_D, bool MIXED, bool FLOW>
+template <int RC, bool TWO_D, bool MIXED, bool FLOW, bool COHERENT = FLOW>
 __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a, unsigned char *smem)
 {
     using G = Geo<RC, TWO_D>;
@@ -339,7 +340,7 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
     double *red = reinterpret_cast<double *>(smem + cv.red);
 
     build_tables<RC, TWO_D>(Gm, start, ftab, tid, nthreads);
-    stage_tile<RC, TWO_D, MIXED, FLOW>(R, Gm, w, tile, tlen, start, tid, nthreads);
+    stage_tile<RC, TWO_D, MIXED, COHERENT>(R, Gm, w, tile, tlen, start, tid, nthreads);
 
     // this thread's fixed role
     const int j = tid / tg, tt = tid - (tid / tg) * tg;
@@ -535,17 +536,25 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_flow(const SnFlowArgs
         const int *dl = f.deps + (size_t)item * SN_MAX_DEPS;
         if (tid < dl[0]) {
             const uint32_t *flag = f.done + dl[1 + tid];
-            for (int it = 0; ld_acquire_gpu(flag) < epoch; it++) {
+            int it = 0;
+            for (; ld_acquire_gpu(flag) < epoch; it++) {
                 if (it >= SN_WAIT_LIMIT) {
-                    atomicOr(f.err, 1);
+                    atomicOr(f.err, 1u);
                     break;
                 }
                 __nanosleep(100);
             }
+            if (it) {  // dependency stall statistics
+                atomicAdd(f.err + 1, 1u);
+                atomicAdd(f.err + 2, (unsigned)it);
+            }
         }
         __syncthreads();
         __threadfence();
-        sweep_block<RC, TWO_D, MIXED, true>(f.base.work[item], f.base, smem);
+        if (f.async_stage)
+            sweep_block<RC, TWO_D, MIXED, true, false>(f.base.work[item], f.base, smem);
+        else
+            sweep_block<RC, TWO_D, MIXED, true, true>(f.base.work[item], f.base, smem);
         __syncthreads();
         if (tid == 0) {
             __threadfence();

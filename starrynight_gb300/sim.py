@@ -314,6 +314,12 @@ class Simulation:
         self._ck(lib().sn_gpu_phase_times(self._h, int(n_sweeps), ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)))
         return a.value, b.value, n.value
 
+    def flow_stats(self) -> dict:
+        """Dataflow schedule statistics since the last call (see sn_gpu_flow_stats)."""
+        s = np.zeros(4, np.uint64)
+        self._ck(lib().sn_gpu_flow_stats(self._h, _ptr(s)))
+        return {"dataflow": bool(s[0]), "grid": int(s[1]), "waited_blocks": int(s[2]), "polls": int(s[3])}
+
     def proposals(self, replica: int, sites: np.ndarray, sweep: int) -> np.ndarray:
         sites = np.ascontiguousarray(sites, np.uint32)
         out = np.zeros((sites.size, 4), np.float32)
