@@ -281,6 +281,14 @@ sn_status sn_plan_schedule(int X, int Y, int Z, int cutoff, int mixed_lengths, s
 /* Host-only: 1 if no two sites updated together interact under periodic
  * boundaries (same block colour and site colour within the cutoff). */
 int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *sched);
+/* Host-only check of the dataflow schedule of a replica table (no GPU
+ * needed): plans every replica's blocks as sn_gpu_init would and verifies,
+ * independently of how the lists were built, that every block appears once
+ * and waits exactly on its periodically adjacent blocks of earlier colour,
+ * all earlier in the list (so the persistent sweep cannot deadlock).
+ * stats (nullable, 3 entries): blocks, dependencies, largest dependency
+ * count.  No reference counterpart. */
+sn_status sn_check_flow(const sn_params *params, int n_replicas, const sn_replica_desc *replicas, uint64_t *stats);
 /* Kernel launches issued by this handle so far. */
 sn_status sn_gpu_launch_count(const sn_handle *h, uint64_t *launches);
 /* The handle's CUDA stream as an opaque pointer (for event timing). */

@@ -62,7 +62,8 @@ _P = ctypes.POINTER
 
 
 def library_path() -> str:
-    return _build.lib_path()
+    # SN_GPU_LIB selects another build of the same library (tuning builds)
+    return os.environ.get("SN_GPU_LIB") or _build.lib_path()
 
 
 def lib() -> ctypes.CDLL:
@@ -102,6 +103,7 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_schedule": ([h, _i, _P(ScheduleInfo)], _i),
             "sn_plan_schedule": ([_i, _i, _i, _i, _i, _P(ScheduleInfo)], _i),
             "sn_check_schedule": ([_i, _i, _i, _i, _P(ScheduleInfo)], _i),
+            "sn_check_flow": ([_P(Params), _i, _P(ReplicaDesc), _vp], _i),
             "sn_gpu_launch_count": ([h, _P(ctypes.c_uint64)], _i),
             "sn_gpu_stream": ([h], _vp),
             "sn_neighbour_count": ([_i, _i], _i),

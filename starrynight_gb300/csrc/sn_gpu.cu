@@ -46,6 +46,117 @@ const sn_flow_launch_fn k_flow[SN_MAX_CUTOFF + 1] = {nullptr,
                                                       sn_launch_flow_rc6};
 
 const int kSmemLimit = 227 * 1024;
+
+// Unique key of block (bx, by, bz) of replica rep (block indices < 2^14 per axis: the
+// planner's blocks are >= 2 sites and lattice sides < 2^15).  The key must not depend on
+// the replica's block counts: replicas of different shapes share one dataflow list.
+inline uint64_t block_key(int rep, int bx, int by, int bz)
+{
+    return ((uint64_t)rep << 42) | ((uint64_t)bx << 28) | ((uint64_t)by << 14) | (uint64_t)bz;
+}
+
+// Host-side launch plan of a replica table: per block colour and kernel variant (3D, 2D) the work
+// lists of the eight-launch schedule, per replica the list of all its blocks (field passes), and per
+// variant the dataflow list -- the blocks in block-colour order, each with the indices of the adjacent
+// blocks of earlier colour (the blocks whose sites its halo reads and that must finish first).  Items
+// only wait on items earlier in their list, which a running CTA has already taken.
+struct SnPlan {
+    std::vector<SnWork> work;
+    int work_off[16] = {}, work_cnt[16] = {}, work_smem[16] = {}, work_thr[16] = {};
+    std::vector<int> fwork_off, fwork_cnt;
+    int flow_off[2] = {0, 0}, flow_items[2] = {0, 0};
+    std::vector<int> deps;  // SN_MAX_DEPS ints per work entry: count, then list positions
+};
+
+int block_colour(const SnTile &t, const int *c) { return (c[0] % t.m[0]) * 4 + (c[1] % t.m[1]) * 2 + (c[2] % t.m[2]); }
+
+bool build_plan(const std::vector<SnTile> &tiles, const sn_replica_desc *replicas, int n, bool flow, SnPlan &pl,
+                std::string &why)
+{
+    std::vector<SnWork> &work = pl.work;
+    for (int p = 0; p < 8; p++)
+        for (int v = 0; v < 2; v++) {
+            const int k = p * 2 + v;
+            pl.work_off[k] = (int)work.size();
+            const int cb[3] = {(p >> 2) & 1, (p >> 1) & 1, p & 1};
+            for (int r = 0; r < n; r++) {
+                const bool two_d = replicas[r].Z == 1;
+                if ((v == 1) != two_d) continue;
+                const SnTile &t = tiles[r];
+                for (int bx = 0; bx < t.nb[0]; bx++)
+                    for (int by = 0; by < t.nb[1]; by++)
+                        for (int bz = 0; bz < t.nb[2]; bz++) {
+                            if (bx % t.m[0] != cb[0] || by % t.m[1] != cb[1] || bz % t.m[2] != cb[2]) continue;
+                            work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
+                            pl.work_smem[k] = std::max(pl.work_smem[k], t.smem_bytes);
+                            pl.work_thr[k] = std::max(pl.work_thr[k], t.threads);
+                        }
+            }
+            pl.work_cnt[k] = (int)work.size() - pl.work_off[k];
+        }
+    pl.fwork_off.assign(n, 0);
+    pl.fwork_cnt.assign(n, 0);
+    for (int r = 0; r < n; r++) {
+        const SnTile &t = tiles[r];
+        pl.fwork_off[r] = (int)work.size();
+        for (int bx = 0; bx < t.nb[0]; bx++)
+            for (int by = 0; by < t.nb[1]; by++)
+                for (int bz = 0; bz < t.nb[2]; bz++) work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
+        pl.fwork_cnt[r] = (int)work.size() - pl.fwork_off[r];
+    }
+    std::vector<int> &deps = pl.deps;
+    for (int v = 0; v < 2 && flow; v++) {
+        pl.flow_off[v] = (int)work.size();
+        std::unordered_map<uint64_t, int> index;  // (replica, block) -> position in this list
+        for (int p = 0; p < 8; p++) {
+            const int k = p * 2 + v;
+            for (int i = 0; i < pl.work_cnt[k]; i++) {
+                const SnWork w = work[pl.work_off[k] + i];
+                const SnTile &t = tiles[w.rep];
+                index[block_key(w.rep, w.x0 / t.B[0], w.y0 / t.B[1], w.z0 / t.B[2])] = (int)work.size() - pl.flow_off[v];
+                work.push_back(w);
+            }
+        }
+        pl.flow_items[v] = (int)work.size() - pl.flow_off[v];
+        deps.resize((size_t)(pl.flow_off[v] + pl.flow_items[v]) * SN_MAX_DEPS, 0);
+        for (int i = 0; i < pl.flow_items[v]; i++) {
+            const SnWork w = work[pl.flow_off[v] + i];
+            const SnTile &t = tiles[w.rep];
+            const int b[3] = {w.x0 / t.B[0], w.y0 / t.B[1], w.z0 / t.B[2]};
+            const int own = block_colour(t, b);
+            int *dl = &deps[(size_t)(pl.flow_off[v] + i) * SN_MAX_DEPS];
+            for (int dx = -1; dx <= 1; dx++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dz = -1; dz <= 1; dz++) {
+                        const int c[3] = {(b[0] + dx + t.nb[0]) % t.nb[0], (b[1] + dy + t.nb[1]) % t.nb[1],
+                                          (b[2] + dz + t.nb[2]) % t.nb[2]};
+                        if (c[0] == b[0] && c[1] == b[1] && c[2] == b[2]) continue;
+                        const int q = block_colour(t, c);
+                        if (q == own) {
+                            why = "adjacent blocks share a colour";
+                            return false;
+                        }
+                        if (q > own) continue;
+                        const auto it = index.find(block_key(w.rep, c[0], c[1], c[2]));
+                        if (it == index.end()) {
+                            why = "dataflow list misses a block";
+                            return false;
+                        }
+                        const int j = it->second;
+                        bool seen = false;
+                        for (int u = 1; u <= dl[0]; u++) seen |= dl[u] == j;
+                        if (seen) continue;
+                        if (dl[0] + 1 >= SN_MAX_DEPS) {
+                            why = "too many dependencies";
+                            return false;
+                        }
+                        dl[++dl[0]] = j;
+                    }
+        }
+    }
+    if (flow) deps.resize(work.size() * SN_MAX_DEPS, 0);
+    return true;
+}
 // the sweep kernels' static shared memory (the dataflow queue slot) comes on top of the planned tile
 const int kSweepStatic = 128;
 // per-block shared memory that still lets two blocks share an SM (228 KB per
@@ -199,7 +310,7 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
             t.threads = NS * t.tg;
             t.ng = ng;
             t.merge = merge;
-            if (t.threads > (pass == 0 ? SN_MAX_THREADS / 2 : SN_MAX_THREADS)) continue;
+            if (t.threads > (pass == 0 ? SN_TWO_PER_SM_THREADS : SN_SWEEP_MAX_THREADS)) continue;
             const int pc_min = pass == 0 ? std::min(8, ng) : 1;
             // quick lower bound on shared memory with no padding
             if ((int)sn_sweep::sn_carve(t.T[0] * t.T[1] * t.T[2], t.tg, pc_min, NS, S, NF, mixed, 4).total > limit)
@@ -312,7 +423,6 @@ struct sn_handle {
     size_t done_n = 0;
     uint32_t *d_queue = nullptr;  // 2 counters
     uint32_t *d_err = nullptr;    // timeout flag, stall statistics
-    int flow_async = 1;
     std::vector<float *> lattice_mem;
     // scratch (lazy)
     float *d_stage = nullptr;
@@ -449,7 +559,6 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
             f.done = h->d_done + h->flow_off[v];
             f.queue = h->d_queue + v;
             f.err = h->d_err;
-            f.async_stage = h->flow_async;
             int thr = 0, smem = 0;
             for (int p = 0; p < 8; p++) {
                 thr = std::max(thr, h->work_thr[p * 2 + v]);
@@ -594,6 +703,84 @@ sn_status sn_plan_schedule(int X, int Y, int Z, int cutoff, int mixed_lengths, s
     return SN_OK;
 }
 
+sn_status sn_check_flow(const sn_params *params, int n_replicas, const sn_replica_desc *replicas, uint64_t *stats)
+{
+    if (!params || !replicas || n_replicas < 1) return fail(nullptr, SN_ERR_ARG, "null argument or no replicas");
+    const sn_params &P = *params;
+    if (P.cutoff < 1 || P.cutoff > SN_MAX_CUTOFF)
+        return fail(nullptr, SN_ERR_UNSUPPORTED, "cutoff %d outside 1..%d", P.cutoff, SN_MAX_CUTOFF);
+    float L = 0.0f;
+    bool mixed = false;
+    for (int i = 0; i < P.n_species && i < SN_MAX_SPECIES; i++)
+        if (P.dipoles[i] > 0.0f) {
+            if (L == 0.0f) L = P.dipoles[i];
+            else if (P.dipoles[i] != L) mixed = true;
+        }
+    std::vector<SnTile> tiles(n_replicas);
+    std::string why;
+    for (int r = 0; r < n_replicas; r++)
+        if (!plan_tile(replicas[r].X, replicas[r].Y, replicas[r].Z, P.cutoff, mixed, tiles[r], why))
+            return fail(nullptr, SN_ERR_SCHEDULE, "replica %d: %s", r, why.c_str());
+    SnPlan pl;
+    if (!build_plan(tiles, replicas, n_replicas, true, pl, why)) return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
+    // Independent check of the dataflow lists (direct block grids, not the key map):
+    // every block once; dependencies earlier in the list, of the same replica, adjacent
+    // (periodically) and of an earlier colour; every such neighbour present.
+    uint64_t items = 0, ndeps = 0, maxd = 0;
+    for (int v = 0; v < 2; v++) {
+        std::vector<std::vector<int>> pos(n_replicas);
+        for (int r = 0; r < n_replicas; r++)
+            if ((replicas[r].Z == 1) == (v == 1)) pos[r].assign((size_t)tiles[r].nb[0] * tiles[r].nb[1] * tiles[r].nb[2], -1);
+        auto cell = [&](int r, const int *c) -> int & {
+            const SnTile &t = tiles[r];
+            return pos[r][((size_t)c[0] * t.nb[1] + c[1]) * t.nb[2] + c[2]];
+        };
+        for (int i = 0; i < pl.flow_items[v]; i++) {
+            const SnWork &w = pl.work[pl.flow_off[v] + i];
+            const SnTile &t = tiles[w.rep];
+            const int b[3] = {w.x0 / t.B[0], w.y0 / t.B[1], w.z0 / t.B[2]};
+            if (pos[w.rep].empty() || cell(w.rep, b) != -1)
+                return fail(nullptr, SN_ERR_SCHEDULE, "block listed twice or in the wrong variant");
+            cell(w.rep, b) = i;
+        }
+        for (int r = 0; r < n_replicas; r++)
+            for (int p : pos[r])
+                if (p < 0) return fail(nullptr, SN_ERR_SCHEDULE, "replica %d: a block is missing", r);
+        for (int i = 0; i < pl.flow_items[v]; i++) {
+            const SnWork &w = pl.work[pl.flow_off[v] + i];
+            const SnTile &t = tiles[w.rep];
+            const int b[3] = {w.x0 / t.B[0], w.y0 / t.B[1], w.z0 / t.B[2]};
+            const int own = block_colour(t, b);
+            const int *dl = &pl.deps[(size_t)(pl.flow_off[v] + i) * SN_MAX_DEPS];
+            std::vector<int> want;
+            for (int dx = -1; dx <= 1; dx++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dz = -1; dz <= 1; dz++) {
+                        const int c[3] = {(b[0] + dx + t.nb[0]) % t.nb[0], (b[1] + dy + t.nb[1]) % t.nb[1],
+                                          (b[2] + dz + t.nb[2]) % t.nb[2]};
+                        if ((c[0] == b[0] && c[1] == b[1] && c[2] == b[2]) || block_colour(t, c) > own) continue;
+                        want.push_back(cell(w.rep, c));
+                    }
+            std::sort(want.begin(), want.end());
+            want.erase(std::unique(want.begin(), want.end()), want.end());
+            std::vector<int> got(dl + 1, dl + 1 + dl[0]);
+            std::sort(got.begin(), got.end());
+            if (got != want) return fail(nullptr, SN_ERR_SCHEDULE, "item %d: dependency list differs", i);
+            for (int j : got)
+                if (j >= i) return fail(nullptr, SN_ERR_SCHEDULE, "item %d waits on a later item", i);
+            ndeps += got.size();
+            maxd = std::max<uint64_t>(maxd, got.size());
+        }
+        items += (uint64_t)pl.flow_items[v];
+    }
+    if (stats) {
+        stats[0] = items;
+        stats[1] = ndeps;
+        stats[2] = maxd;
+    }
+    return SN_OK;
+}
+
 int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *sc)
 {
     if (!sc || X < 1 || Y < 1 || Z < 1 || cutoff < 1) return 0;
@@ -657,7 +844,8 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     }
     for (int r = 0; r < n_replicas; r++) {
         const sn_replica_desc &d = replicas[r];
-        if (d.X < 1 || d.Y < 1 || d.Z < 1) return fail(nullptr, SN_ERR_ARG, "replica %d: bad size", r);
+        if (d.X < 1 || d.Y < 1 || d.Z < 1 || d.X >= (1 << 15) || d.Y >= (1 << 15) || d.Z >= (1 << 15))
+            return fail(nullptr, SN_ERR_ARG, "replica %d: bad size (each side 1 .. 32767)", r);
         if ((long long)d.X * d.Y * d.Z > 0x7fffffffLL)
             return fail(nullptr, SN_ERR_UNSUPPORTED, "replica %d: more than 2^31-1 sites", r);
         if (!(d.T > 0.0f)) return fail(nullptr, SN_ERR_ARG, "replica %d: temperature must be > 0", r);
@@ -724,88 +912,27 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         R.seed_hi = (uint32_t)(seed >> 32);
     }
 
-    // work lists: per block colour and kernel variant (3D, 2D), then all blocks per replica
-    std::vector<SnWork> work;
-    for (int p = 0; p < 8; p++)
-        for (int v = 0; v < 2; v++) {
-            const int k = p * 2 + v;
-            h->work_off[k] = (int)work.size();
-            const int cb[3] = {(p >> 2) & 1, (p >> 1) & 1, p & 1};
-            for (int r = 0; r < n_replicas; r++) {
-                const bool two_d = replicas[r].Z == 1;
-                if ((v == 1) != two_d) continue;
-                const SnTile &t = h->tiles[r];
-                for (int bx = 0; bx < t.nb[0]; bx++)
-                    for (int by = 0; by < t.nb[1]; by++)
-                        for (int bz = 0; bz < t.nb[2]; bz++) {
-                            if (bx % t.m[0] != cb[0] || by % t.m[1] != cb[1] || bz % t.m[2] != cb[2]) continue;
-                            work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
-                            h->work_smem[k] = std::max(h->work_smem[k], t.smem_bytes);
-                            h->work_thr[k] = std::max(h->work_thr[k], t.threads);
-                        }
-            }
-            h->work_cnt[k] = (int)work.size() - h->work_off[k];
-        }
-    for (int r = 0; r < n_replicas; r++) {
-        const SnTile &t = h->tiles[r];
-        h->fwork_off[r] = (int)work.size();
-        for (int bx = 0; bx < t.nb[0]; bx++)
-            for (int by = 0; by < t.nb[1]; by++)
-                for (int bz = 0; bz < t.nb[2]; bz++) work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
-        h->fwork_cnt[r] = (int)work.size() - h->fwork_off[r];
-    }
-
-    // dataflow lists: per kernel variant, the blocks in block-colour order, each with the indices of the
-    // adjacent blocks of earlier colour (the blocks whose sites its halo reads and that must finish first).
-    // Items only wait on items earlier in their list, which a running block has already taken.
-    std::vector<int> deps;
     if (const char *env = getenv("SN_SCHEDULE")) h->flow = strcmp(env, "phases") != 0;
-    if (const char *env = getenv("SN_FLOW_STAGE")) h->flow_async = strcmp(env, "coherent") != 0;
-    for (int v = 0; v < 2 && h->flow; v++) {
-        h->flow_off[v] = (int)work.size();
-        std::unordered_map<uint64_t, int> index;  // (replica, block) -> position in this list
-        for (int p = 0; p < 8; p++) {
-            const int k = p * 2 + v;
-            for (int i = 0; i < h->work_cnt[k]; i++) {
-                const SnWork w = work[h->work_off[k] + i];
-                const SnTile &t = h->tiles[w.rep];
-                const uint64_t key = (((uint64_t)w.rep * t.nb[0] + w.x0 / t.B[0]) * t.nb[1] + w.y0 / t.B[1]) *
-                                         t.nb[2] + w.z0 / t.B[2];
-                index[key] = (int)work.size() - h->flow_off[v];
-                work.push_back(w);
-            }
-        }
-        h->flow_items[v] = (int)work.size() - h->flow_off[v];
-        deps.resize((size_t)(h->flow_off[v] + h->flow_items[v]) * SN_MAX_DEPS, 0);
-        for (int i = 0; i < h->flow_items[v]; i++) {
-            const SnWork w = work[h->flow_off[v] + i];
-            const SnTile &t = h->tiles[w.rep];
-            const int b[3] = {w.x0 / t.B[0], w.y0 / t.B[1], w.z0 / t.B[2]};
-            auto colour = [&](const int *c) {
-                return (c[0] % t.m[0]) * 4 + (c[1] % t.m[1]) * 2 + (c[2] % t.m[2]);
-            };
-            const int own = colour(b);
-            int *dl = &deps[(size_t)(h->flow_off[v] + i) * SN_MAX_DEPS];
-            for (int dx = -1; dx <= 1; dx++)
-                for (int dy = -1; dy <= 1; dy++)
-                    for (int dz = -1; dz <= 1; dz++) {
-                        const int c[3] = {(b[0] + dx + t.nb[0]) % t.nb[0], (b[1] + dy + t.nb[1]) % t.nb[1],
-                                          (b[2] + dz + t.nb[2]) % t.nb[2]};
-                        if (c[0] == b[0] && c[1] == b[1] && c[2] == b[2]) continue;
-                        const int q = colour(c);
-                        if (q == own) return bail(fail(h, SN_ERR_SCHEDULE, "adjacent blocks share a colour"));
-                        if (q > own) continue;
-                        const uint64_t key = (((uint64_t)w.rep * t.nb[0] + c[0]) * t.nb[1] + c[1]) * t.nb[2] + c[2];
-                        const int j = index.at(key);
-                        bool seen = false;
-                        for (int u = 1; u <= dl[0]; u++) seen |= dl[u] == j;
-                        if (seen) continue;
-                        if (dl[0] + 1 >= SN_MAX_DEPS) return bail(fail(h, SN_ERR_SCHEDULE, "too many dependencies"));
-                        dl[++dl[0]] = j;
-                    }
-        }
+    SnPlan plan;
+    {
+        std::string why;
+        if (!build_plan(h->tiles, replicas, n_replicas, h->flow, plan, why))
+            return bail(fail(h, SN_ERR_SCHEDULE, "%s", why.c_str()));
     }
-    if (h->flow) deps.resize(work.size() * SN_MAX_DEPS, 0);
+    for (int k = 0; k < 16; k++) {
+        h->work_off[k] = plan.work_off[k];
+        h->work_cnt[k] = plan.work_cnt[k];
+        h->work_smem[k] = plan.work_smem[k];
+        h->work_thr[k] = plan.work_thr[k];
+    }
+    h->fwork_off = plan.fwork_off;
+    h->fwork_cnt = plan.fwork_cnt;
+    for (int v = 0; v < 2; v++) {
+        h->flow_off[v] = plan.flow_off[v];
+        h->flow_items[v] = plan.flow_items[v];
+    }
+    const std::vector<SnWork> &work = plan.work;
+    const std::vector<int> &deps = plan.deps;
 
     // temperature ladder for exchange: replicas sorted by T
     std::vector<int> order(n_replicas);

@@ -10,6 +10,17 @@
 #include <cstdint>
 
 #define SN_MAX_THREADS 512       // largest sweep / field block
+// Stencil pairs per thread (sets the number of splits) and the threads of a
+// block that shares its SM with a second one (their registers must fit the
+// register file twice).  Build-time tuning knobs.
+#ifndef SN_PAIRS_PER_SPLIT
+#define SN_PAIRS_PER_SPLIT 15
+#endif
+#ifndef SN_TWO_PER_SM_THREADS
+#define SN_TWO_PER_SM_THREADS 256
+#endif
+#define SN_SWEEP_MIN_BLOCKS (SN_TWO_PER_SM_THREADS > 256 ? 2 : 1)
+#define SN_SWEEP_MAX_THREADS (SN_TWO_PER_SM_THREADS > 256 ? SN_TWO_PER_SM_THREADS : SN_MAX_THREADS)
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log
 
@@ -97,8 +108,7 @@ struct SnFlowArgs {
     const int *deps;
     uint32_t *done;
     uint32_t *queue;
-    uint32_t *err;    // [0] wait timed out, [1] items that waited, [2] polls
-    int async_stage;  // stage tiles with cp.async (1) or L1-bypassing loads (0)
+    uint32_t *err;  // [0] wait timed out, [1] items that waited, [2] polls
 };
 
 // Neighbour offset table for the per-site kernels (energy, adjoint, quench).

@@ -45,8 +45,9 @@ struct Geo {
     static constexpr int SZ = TWO_D ? 1 : S;         // site colours along z
     static constexpr int NF = 2 * RC + 1;            // offsets per axis
     static constexpr int NP = sn_stencil::npairs(RC, TWO_D);
-    // neighbour-list splits: about 15 +-o pairs per thread, at most 8
-    static constexpr int NS = (NP + 7) / 15 < 1 ? 1 : ((NP + 7) / 15 > 8 ? 8 : (NP + 7) / 15);
+    // neighbour-list splits: about SN_PAIRS_PER_SPLIT +-o pairs per thread, at most 8
+    static constexpr int NSR = (NP + SN_PAIRS_PER_SPLIT / 2) / SN_PAIRS_PER_SPLIT;
+    static constexpr int NS = NSR < 1 ? 1 : (NSR > 8 ? 8 : NSR);
     // Site colours c and c + (s/2, s/2, s/2) never interact when every
     // component of the displacement between their sites is >= s/2, i.e. when
     // 3 (s/2)^2 > cutoff^2 (cutoff 1, 3, 5 in 3D).  They are then updated
@@ -258,12 +259,11 @@ __device__ __forceinline__ void build_tables(const SnTile &Gm, int *start, int *
     }
 }
 
-// Copy of block + halo (periodic wrap) into the class-major tile, by
-// asynchronous copies through L1, or (COHERENT) by loads that bypass L1.  The
-// dataflow kernel reads blocks other SMs wrote during the same launch; its
-// acquire of their done flags followed by a gpu-scope fence orders those
-// writes before either kind of load.
-template <int RC, bool TWO_D, bool MIXED, bool COHERENT = false>
+// Copy of block + halo (periodic wrap) into the class-major tile by
+// asynchronous copies.  The dataflow kernel reads blocks other SMs wrote
+// during the same launch; its acquire of their done flags followed by a
+// gpu-scope fence orders those writes before these copies.
+template <int RC, bool TWO_D, bool MIXED>
 __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, float *tile,
                                            float *tlen, const int *start, int tid, int nthreads)
 {
@@ -281,18 +281,10 @@ __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &
             const int gz = TWO_D ? 0 : sn_wrap(w.z0 - HZ + uz, Z);
             const long long g = gb + gz;
             const int slot = rslot + uz;  // z is stored plainly
-            if constexpr (COHERENT) {
-                const float x = __ldcg(R.px + g), y = __ldcg(R.py + g), z = __ldcg(R.pz + g);
-                tile[3 * slot + 0] = x;
-                tile[3 * slot + 1] = y;
-                tile[3 * slot + 2] = z;
-                if constexpr (MIXED) tlen[slot] = __ldg(R.len + g);  // lengths never change in a sweep
-            } else {
-                cp_async4(&tile[3 * slot + 0], R.px + g);
-                cp_async4(&tile[3 * slot + 1], R.py + g);
-                cp_async4(&tile[3 * slot + 2], R.pz + g);
-                if constexpr (MIXED) cp_async4(&tlen[slot], R.len + g);
-            }
+            cp_async4(&tile[3 * slot + 0], R.px + g);
+            cp_async4(&tile[3 * slot + 1], R.py + g);
+            cp_async4(&tile[3 * slot + 2], R.pz + g);
+            if constexpr (MIXED) cp_async4(&tlen[slot], R.len + g);
         }
     }
 }
@@ -302,7 +294,7 @@ __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &
 // tt = tid % tg of every colour group: half h = tt / tp of the group, target
 // t = tt % tp = (qx, qy, qz) of that colour (inactive where the colour has
 // fewer targets).  Threads with j == 0 also finalize their target.
-template <int RC, bool TWO_D, bool MIXED, bool FLOW, bool COHERENT = FLOW>
+template <int RC, bool TWO_D, bool MIXED, bool FLOW>
 __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a, unsigned char *smem)
 {
     using G = Geo<RC, TWO_D>;
@@ -340,7 +332,7 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
     double *red = reinterpret_cast<double *>(smem + cv.red);
 
     build_tables<RC, TWO_D>(Gm, start, ftab, tid, nthreads);
-    stage_tile<RC, TWO_D, MIXED, COHERENT>(R, Gm, w, tile, tlen, start, tid, nthreads);
+    stage_tile<RC, TWO_D, MIXED>(R, Gm, w, tile, tlen, start, tid, nthreads);
 
     // this thread's fixed role
     const int j = tid / tg, tt = tid - (tid / tg) * tg;
@@ -493,7 +485,7 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
 
 // One block colour per launch, one CTA per block.
 template <int RC, bool TWO_D, bool MIXED>
-__global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_phase(const SnPhaseArgs a)
+__global__ void __launch_bounds__(SN_SWEEP_MAX_THREADS, SN_SWEEP_MIN_BLOCKS) sweep_phase(const SnPhaseArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     sweep_block<RC, TWO_D, MIXED, false>(a.work[blockIdx.x], a, smem);
@@ -521,7 +513,7 @@ __device__ __forceinline__ void st_release_gpu(uint32_t *p, uint32_t v)
 // cannot occur: a block waited on was taken from the queue earlier by a CTA
 // that is running, and it only waits on blocks taken before it.
 template <int RC, bool TWO_D, bool MIXED>
-__global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_flow(const SnFlowArgs f)
+__global__ void __launch_bounds__(SN_SWEEP_MAX_THREADS, SN_SWEEP_MIN_BLOCKS) sweep_flow(const SnFlowArgs f)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_item;
@@ -551,10 +543,7 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) sweep_flow(const SnFlowArgs
         }
         __syncthreads();
         __threadfence();
-        if (f.async_stage)
-            sweep_block<RC, TWO_D, MIXED, true, false>(f.base.work[item], f.base, smem);
-        else
-            sweep_block<RC, TWO_D, MIXED, true, true>(f.base.work[item], f.base, smem);
+        sweep_block<RC, TWO_D, MIXED, true>(f.base.work[item], f.base, smem);
         __syncthreads();
         if (tid == 0) {
             __threadfence();
@@ -588,7 +577,7 @@ template <typename R, int RC, bool TWO_D, bool MIXED>
 __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldArgs a)
 {
     using G = Geo<RC, TWO_D>;
-    constexpr int S = G::S, H = G::H, HZ = G::HZ, SZ = G::SZ, NF = G::NF, NS = G::NS;
+    constexpr int S = G::S, H = G::H, HZ = G::HZ, SZ = G::SZ, NF = G::NF, NP = G::NP;
     constexpr bool MERGE = G::MERGE;
     extern __shared__ __align__(16) unsigned char smem[];
 
@@ -606,118 +595,99 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
     const int Sy = Gm.Sy, Sx = Gm.Sx;
     const int tp = Gm.tp, tg = Gm.tg, ng = Gm.ng;
     const int nqy = Gm.nq[1], nqz = Gm.nq[2];
-    const double C = a.cage, Kk = a.K;
-    const double Ex = Rp.E[0], Ey = Rp.E[1], Ez = Rp.E[2];
+    const R C = (R)a.cage, Kk = (R)a.K;
+    const R Ex = (R)Rp.E[0], Ey = (R)Rp.E[1], Ez = (R)Rp.E[2];
     const R Lu = (R)Rp.length;
 
-    const Carve cv = sn_carve(Gm.slots, tg, 0, NS, S, NF, MIXED, (int)sizeof(R));
-    float *tile = reinterpret_cast<float *>(smem + cv.tile);
+    const Carve cv = sn_carve(Gm.slots, tg, 0, G::NS, S, NF, MIXED, (int)sizeof(R));
     float *tlen = reinterpret_cast<float *>(smem + cv.tlen);
-    R *parts = reinterpret_cast<R *>(smem + cv.parts);
     int *ftab = reinterpret_cast<int *>(smem + cv.ftab);
     int *start = reinterpret_cast<int *>(smem + cv.start);
     double *red = reinterpret_cast<double *>(smem + cv.red);
 
     build_tables<RC, TWO_D>(Gm, start, ftab, tid, nthreads);
-    stage_tile<RC, TWO_D, MIXED>(Rp, Gm, w, tile, tlen, start, tid, nthreads);
+    stage_tile<RC, TWO_D, MIXED>(Rp, Gm, w, reinterpret_cast<float *>(smem + cv.tile), tlen, start, tid, nthreads);
     cp_async_wait_all();
     __syncthreads();
 
-    const int j = tid / tg, tt = tid - (tid / tg) * tg;
-    const int hh = tt / tp, t = tt - (tt / tp) * tp;
-    const int qz = t % nqz, qy = (t / nqz) % nqy, qx = t / (nqz * nqy);
-    const bool tvalid = tid < NS * tg && qx < Gm.nq[0];
-    const int trel = qx * Sx + qy * Sy + S * qz;  // z plain: targets S apart
-    const int srel = ((S * qx) * Y + S * qy) * Z + (TWO_D ? 0 : S * qz);
-
+    // Read-only pass: every (colour group, target) of the block is an
+    // independent item; a thread runs the whole stencil of its items, so the
+    // loop needs no barrier.  Lanes of a warp take consecutive targets of one
+    // group, the conflict-free pattern of the tile layout.
     double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    int FX[NF], FY[NF];
-    int pcx = -1, pcy = -1;
-    for (int g = 0; g < ng; g++) {
+    const int items = ng * tg;
+    for (int it = tid; it < items; it += nthreads) {
+        const int g = it / tg, tt = it - (it / tg) * tg;
+        const int hh = tt / tp, t = tt - (tt / tp) * tp;
+        const int qz = t % nqz, qy = (t / nqz) % nqy, qx = t / (nqz * nqy);
         int cx, cy, cz;
         group_colour<S, SZ, MERGE>(g, hh, cx, cy, cz);
-        const bool active = tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
-                            (TWO_D || qz < sn_count(Bz, cz, S));
-        if (cx != pcx) {
+        if (!(qx < Gm.nq[0] && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
+              (TWO_D || qz < sn_count(Bz, cz, S))))
+            continue;
+        int FX[NF], FY[NF];
 #pragma unroll
-            for (int o = 0; o < NF; o++) FX[o] = ftab[(0 * S + cx) * NF + o];
-            pcx = cx;
-        }
-        if (cy != pcy) {
-#pragma unroll
-            for (int o = 0; o < NF; o++) FY[o] = ftab[(1 * S + cy) * NF + o];
-            pcy = cy;
+        for (int o = 0; o < NF; o++) {
+            FX[o] = ftab[(0 * S + cx) * NF + o];
+            FY[o] = ftab[(1 * S + cy) * NF + o];
         }
         const int tslot = sn_pi<S>(start, cx + H) * Sx + sn_pi<S>(start + SN_MAX_S, cy + H) * Sy +
-                          (TWO_D ? 0 : cz + HZ) + trel;
-        if (active) {
-            R hacc[2][3] = {{0, 0, 0}, {0, 0, 0}};
-            R nn[3] = {0, 0, 0};
-            dispatch_split<R, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, (uint32_t)tslot * 12u, FX, FY, tlen,
-                                                   (uint32_t)tslot, hacc, nn);
-            R *pp = parts + (j * 6) * tg + tt;
-            pp[0 * tg] = hacc[0][0] + hacc[1][0];
-            pp[1 * tg] = hacc[0][1] + hacc[1][1];
-            pp[2 * tg] = hacc[0][2] + hacc[1][2];
-            pp[3 * tg] = nn[0];
-            pp[4 * tg] = nn[1];
-            pp[5 * tg] = nn[2];
+                          (TWO_D ? 0 : cz + HZ) + qx * Sx + qy * Sy + S * qz;
+        R hacc[2][3] = {{0, 0, 0}, {0, 0, 0}};
+        R nnv[3] = {0, 0, 0};
+        if constexpr (sizeof(R) == 4) {
+            run_pairs<R, RC, TWO_D, MIXED, 0>(std::make_integer_sequence<int, NP>{}, smem + cv.tile,
+                                              (uint32_t)tslot * 12u, FX, FY, tlen, (uint32_t)tslot, hacc, nnv);
+        } else {
+            // FP64 validation mode: one stencil slice at a time keeps the double registers in check
+#pragma unroll 1
+            for (int j = 0; j < G::NS; j++)
+                dispatch_split<R, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, (uint32_t)tslot * 12u, FX, FY, tlen,
+                                                       (uint32_t)tslot, hacc, nnv);
         }
-        __syncthreads();
-        if (j == 0 && active) {
-            R hx = 0, hy = 0, hz = 0, nx = 0, ny = 0, nz = 0;
-#pragma unroll
-            for (int k = 0; k < NS; k++) {
-                const R *pp = parts + (k * 6) * tg + tt;
-                hx += pp[0 * tg];
-                hy += pp[1 * tg];
-                hz += pp[2 * tg];
-                nx += pp[3 * tg];
-                ny += pp[4 * tg];
-                nz += pp[5 * tg];
+        const R hx = hacc[0][0] + hacc[1][0], hy = hacc[0][1] + hacc[1][1], hz = hacc[0][2] + hacc[1][2];
+        const long long site = ((long long)(w.x0 + cx + S * qx) * Y + (w.y0 + cy + S * qy)) * Z +
+                               (TWO_D ? 0 : w.z0 + cz + S * qz);
+        const R px = (R)gpx[site], py = (R)gpy[site], pz = (R)gpz[site];
+        const R Li = (R)glen[site];  // 0 at vacancies in both modes
+        if (Li == R(0)) {
+            if (a.site_e) a.site_e[site] = 0.0;
+            if (a.grad) {
+                a.grad[3 * site + 0] = 0.0f;
+                a.grad[3 * site + 1] = 0.0f;
+                a.grad[3 * site + 2] = 0.0f;
             }
-            const long long site = ((long long)(w.x0 + cx) * Y + (w.y0 + cy)) * Z + (TWO_D ? 0 : w.z0 + cz) + srel;
-            const double px = gpx[site], py = gpy[site], pz = gpz[site];
-            const double Li = (double)glen[site];  // 0 at vacancies in both modes
-            if (Li == 0.0) {
-                if (a.site_e) a.site_e[site] = 0.0;
-                if (a.grad) {
-                    a.grad[3 * site + 0] = 0.0f;
-                    a.grad[3 * site + 1] = 0.0f;
-                    a.grad[3 * site + 2] = 0.0f;
-                }
-            } else {
-                // H = sum_j len_j T p_j: uniform tiles hold unit p (H = L h)
-                const R sc = MIXED ? R(1) : Lu;
-                const double Hx = (double)(sc * hx), Hy = (double)(sc * hy), Hz = (double)(sc * hz);
-                const double gx = Li * Hx - C * (double)nx + Ex;
-                const double gy = Li * Hy - C * (double)ny + Ey;
-                const double gz = Li * Hz - C * (double)nz + Ez;
-                const double kt = Kk > 0.0 ? -Kk * (fabs(px) + fabs(py)) : 0.0;
-                const double pH = px * Hx + py * Hy + pz * Hz;
-                const double pn = px * (double)nx + py * (double)ny + pz * (double)nz;
-                const double pE = px * Ex + py * Ey + pz * Ez;
-                if (a.site_e) a.site_e[site] = px * gx + py * gy + pz * gz + kt;
-                if (a.grad) {
-                    const double sx = Kk > 0.0 ? (px > 0.0 ? 1.0 : (px < 0.0 ? -1.0 : 0.0)) : 0.0;
-                    const double sy = Kk > 0.0 ? (py > 0.0 ? 1.0 : (py < 0.0 ? -1.0 : 0.0)) : 0.0;
-                    a.grad[3 * site + 0] = (float)(gx - Kk * sx);
-                    a.grad[3 * site + 1] = (float)(gy - Kk * sy);
-                    a.grad[3 * site + 2] = (float)gz;
-                }
-                acc[0] += 0.5 * Li * pH;
-                acc[1] += pn;
-                acc[2] += pE;
-                acc[3] += kt;
-                acc[4] += Li * px;
-                acc[5] += Li * py;
-                acc[6] += Li * pz;
-                acc[7] += px;
-                acc[8] += py;
-                acc[9] += pz;
-            }
+            continue;
         }
-        __syncthreads();
+        // H = sum_j len_j T p_j: uniform tiles hold unit p (H = L h).  Site
+        // products in R (FP32 fields: FP32 products, FP64 sums)
+        const R sc = MIXED ? R(1) : Lu;
+        const R Hx = sc * hx, Hy = sc * hy, Hz = sc * hz;
+        const R gx = Li * Hx - C * nnv[0] + Ex;
+        const R gy = Li * Hy - C * nnv[1] + Ey;
+        const R gz = Li * Hz - C * nnv[2] + Ez;
+        const R kt = Kk > R(0) ? -Kk * (fabs(px) + fabs(py)) : R(0);
+        const R pH = px * Hx + py * Hy + pz * Hz;
+        const R pn = px * nnv[0] + py * nnv[1] + pz * nnv[2];
+        const R pE = px * Ex + py * Ey + pz * Ez;
+        if (a.site_e) a.site_e[site] = (double)(px * gx + py * gy + pz * gz + kt);
+        if (a.grad) {
+            const R sx = Kk > R(0) ? (px > R(0) ? R(1) : (px < R(0) ? R(-1) : R(0))) : R(0);
+            const R sy = Kk > R(0) ? (py > R(0) ? R(1) : (py < R(0) ? R(-1) : R(0))) : R(0);
+            a.grad[3 * site + 0] = (float)(gx - Kk * sx);
+            a.grad[3 * site + 1] = (float)(gy - Kk * sy);
+            a.grad[3 * site + 2] = (float)gz;
+        }
+        acc[0] += 0.5 * (double)(Li * pH);
+        acc[1] += (double)pn;
+        acc[2] += (double)pE;
+        acc[3] += (double)kt;
+        acc[4] += (double)(Li * px);
+        acc[5] += (double)(Li * py);
+        acc[6] += (double)(Li * pz);
+        acc[7] += (double)px;
+        acc[8] += (double)py;
+        acc[9] += (double)pz;
     }
 #pragma unroll
     for (int k = 0; k < 10; k++) acc[k] = warp_sum(acc[k]);

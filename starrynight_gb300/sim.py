@@ -90,6 +90,15 @@ def check_schedule(X: int, Y: int, Z: int, cutoff: int, sched: dict) -> bool:
     return bool(lib().sn_check_schedule(X, Y, Z, cutoff, ctypes.byref(info)))
 
 
+def check_flow(params: "ModelParams", replicas: Sequence["Replica"]) -> dict:
+    """Host-only verification of the dataflow schedule of a replica table (raises on a defect)."""
+    cp = params.to_c()
+    arr = (_abi.ReplicaDesc * len(replicas))(*[r.to_c() for r in replicas])
+    st = np.zeros(3, np.uint64)
+    check(lib().sn_check_flow(ctypes.byref(cp), len(replicas), arr, _ptr(st)))
+    return {"blocks": int(st[0]), "dependencies": int(st[1]), "max_dependencies": int(st[2])}
+
+
 def fp32_peak():
     """(measured FP32 TFLOP/s on the current device, nominal max SM clock MHz)."""
     t, c = ctypes.c_double(0.0), ctypes.c_double(0.0)

@@ -3,6 +3,7 @@ point declared in include/sn_gpu.h, and its host-only planner produces
 conflict-free schedules.  No compute call is made here."""
 import ctypes
 
+import numpy as np
 import pytest
 
 import starrynight_gb300 as sn
@@ -64,3 +65,29 @@ def test_planner_reports_unschedulable_lattices(native_lib, shape, rc):
     with pytest.raises(sn.SnError) as e:
         sn.plan_schedule(*shape, rc)
     assert e.value.name in ("SN_ERR_SCHEDULE", "SN_ERR_UNSUPPORTED")
+
+
+def _flow_tables(sn):
+    rng = np.random.default_rng(777)
+    sizes = rng.choice([32, 48, 64, 96, 128], size=64)
+    uneven = [sn.Replica(int(L), int(L), int(L), T=100.0 + i, seed=i) for i, L in enumerate(sizes)]
+    mixed_2d = [sn.Replica(96, 96, 96, T=300.0)] * 3 + [sn.Replica(2048, 2048, 1, T=300.0),
+                                                         sn.Replica(40, 64, 1, T=200.0)]
+    odd = [sn.Replica(10, 12, 14), sn.Replica(12, 12, 1), sn.Replica(24, 16, 20), sn.Replica(256, 256, 256)]
+    return [("uneven64_rc3", sn.ModelParams(cutoff=3), uneven), ("cubes_and_slabs_rc5", sn.ModelParams(cutoff=5),
+                                                                   mixed_2d),
+            ("small_rc3_mixed", sn.ModelParams(cutoff=3, dipoles=(1.0, 0.5, 0.0), prevalence=(0.5, 0.3, 0.2)), odd),
+            ("rc1", sn.ModelParams(cutoff=1), odd)]
+
+
+def test_dataflow_schedule_is_complete_and_acyclic(native_lib):
+    """Every block of every replica once; each waits exactly on its adjacent blocks of
+    earlier colour, all earlier in the queue -- including tables of replicas of
+    different shapes, whose block indices must not alias."""
+    sn = native_lib
+    for name, params, reps in _flow_tables(sn):
+        st = sn.check_flow(params, reps)
+        assert st["blocks"] == sum(int(np.prod([r.X, r.Y, r.Z])) // int(np.prod(
+            [sn.plan_schedule(r.X, r.Y, r.Z, params.cutoff, mixed=len({d for d in params.dipoles if d > 0}) > 1)[k]
+             for k in ("bx", "by", "bz")])) for r in reps), name
+        assert 0 < st["max_dependencies"] <= 26, name  # the 26 neighbours of a last-colour block
