@@ -192,11 +192,12 @@ def time_sweeps(sim, torch, n):
     sim.sweep(n)
     e1.record(st)
     e1.synchronize()
+    sim.observables()  # raises if a device wait of the timed sweeps gave up (SN_ERR_TIMEOUT)
     return e0.elapsed_time(e1)
 
 
 def run_batched(sn, torch, steps=20):
-    """Batched replica table (64 uneven lattices, one launch per block colour)
+    """Batched replica table (64 uneven lattices swept by the same launches)
     vs the same lattices swept one handle at a time."""
     reps = batched_replicas(sn)
     params = sn.ModelParams(cutoff=BATCHED["cutoff"], cage_strain=1.0, seed=BATCHED["seed"])

@@ -20,6 +20,10 @@
 #define SN_TWO_PER_SM_THREADS 256
 #endif
 #define SN_SWEEP_MIN_BLOCKS (SN_TWO_PER_SM_THREADS > 256 ? 2 : 1)
+// Independent local-field accumulator sets that consecutive stencil pairs rotate through.
+#ifndef SN_ACC_SETS
+#define SN_ACC_SETS 2
+#endif
 #define SN_SWEEP_MAX_THREADS (SN_TWO_PER_SM_THREADS > 256 ? SN_TWO_PER_SM_THREADS : SN_MAX_THREADS)
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log

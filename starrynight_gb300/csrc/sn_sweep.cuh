@@ -59,6 +59,16 @@ struct Geo {
 };
 
 __device__ __forceinline__ float sn_fma(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Sum of component c over the accumulator sets, in set order.
+template <typename R>
+__device__ __forceinline__ R sum_sets(const R (&h)[SN_ACC_SETS][3], int c)
+{
+    R s = h[0][c];
+#pragma unroll
+    for (int k = 1; k < SN_ACC_SETS; k++) s += h[k][c];
+    return s;
+}
 __device__ __forceinline__ double sn_fma(double a, double b, double c) { return fma(a, b, c); }
 
 // ---------------------------------------------------------------------------
@@ -66,7 +76,7 @@ __device__ __forceinline__ double sn_fma(double a, double b, double c) { return 
 template <typename R, int RC, bool TWO_D, bool MIXED, int I>
 __device__ __forceinline__ void pair_step(const unsigned char *__restrict__ base, uint32_t tb,
                                           const int (&FX)[2 * RC + 1], const int (&FY)[2 * RC + 1],
-                                          const float *__restrict__ tlen, uint32_t tslot, R (&h)[2][3],
+                                          const float *__restrict__ tlen, uint32_t tslot, R (&h)[SN_ACC_SETS][3],
                                           R (&nn)[3])
 {
     constexpr sn_stencil::Off o = sn_stencil::pair_offset(RC, TWO_D, I);
@@ -101,7 +111,7 @@ __device__ __forceinline__ void pair_step(const unsigned char *__restrict__ base
     constexpr R txy = (R)sn_stencil::tensor_d(o.x, o.y, o.z, 3);
     constexpr R txz = (R)sn_stencil::tensor_d(o.x, o.y, o.z, 4);
     constexpr R tyz = (R)sn_stencil::tensor_d(o.x, o.y, o.z, 5);
-    R(&a)[3] = h[I & 1];
+    R(&a)[3] = h[I % SN_ACC_SETS];  // independent accumulator chains for consecutive pairs
     a[0] = sn_fma(txx, qx, a[0]);
     if constexpr (txy != 0.0f) a[0] = sn_fma(txy, qy, a[0]);
     if constexpr (txz != 0.0f) a[0] = sn_fma(txz, qz, a[0]);
@@ -128,7 +138,7 @@ __device__ __forceinline__ void pair_step(const unsigned char *__restrict__ base
 template <typename R, int RC, bool TWO_D, bool MIXED, int LO, int... Is>
 __device__ __forceinline__ void run_pairs(std::integer_sequence<int, Is...>, const unsigned char *base, uint32_t tb,
                                           const int (&FX)[2 * RC + 1], const int (&FY)[2 * RC + 1],
-                                          const float *tlen, uint32_t tslot, R (&h)[2][3], R (&nn)[3])
+                                          const float *tlen, uint32_t tslot, R (&h)[SN_ACC_SETS][3], R (&nn)[3])
 {
     (pair_step<R, RC, TWO_D, MIXED, LO + Is>(base, tb, FX, FY, tlen, tslot, h, nn), ...);
 }
@@ -136,7 +146,7 @@ __device__ __forceinline__ void run_pairs(std::integer_sequence<int, Is...>, con
 template <typename R, int RC, bool TWO_D, bool MIXED, int J>
 __device__ __forceinline__ void dispatch_split(int j, const unsigned char *base, uint32_t tb,
                                                const int (&FX)[2 * RC + 1], const int (&FY)[2 * RC + 1],
-                                               const float *tlen, uint32_t tslot, R (&h)[2][3], R (&nn)[3])
+                                               const float *tlen, uint32_t tslot, R (&h)[SN_ACC_SETS][3], R (&nn)[3])
 {
     using G = Geo<RC, TWO_D>;
     if constexpr (J < G::NS) {
@@ -414,15 +424,15 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
 
         // ---- 1. partial g = len_i h - C nn of this split ---------------------------
         if (active) {
-            float hacc[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+            float hacc[SN_ACC_SETS][3] = {};
             float nn[3] = {0.f, 0.f, 0.f};
             dispatch_split<float, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, (uint32_t)tslot * 12u, FX, FY, tlen,
                                                        (uint32_t)tslot, hacc, nn);
             const float sc = MIXED ? tlen[tslot] : Lu * Lu;
             float *pp = parts + (j * 3) * tg + tt;
-            pp[0 * tg] = fmaf(sc, hacc[0][0] + hacc[1][0], -C * nn[0]);
-            pp[1 * tg] = fmaf(sc, hacc[0][1] + hacc[1][1], -C * nn[1]);
-            pp[2 * tg] = fmaf(sc, hacc[0][2] + hacc[1][2], -C * nn[2]);
+            pp[0 * tg] = fmaf(sc, sum_sets(hacc, 0), -C * nn[0]);
+            pp[1 * tg] = fmaf(sc, sum_sets(hacc, 1), -C * nn[1]);
+            pp[2 * tg] = fmaf(sc, sum_sets(hacc, 2), -C * nn[2]);
         }
         __syncthreads();
 
@@ -633,7 +643,7 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
         }
         const int tslot = sn_pi<S>(start, cx + H) * Sx + sn_pi<S>(start + SN_MAX_S, cy + H) * Sy +
                           (TWO_D ? 0 : cz + HZ) + qx * Sx + qy * Sy + S * qz;
-        R hacc[2][3] = {{0, 0, 0}, {0, 0, 0}};
+        R hacc[SN_ACC_SETS][3] = {};
         R nnv[3] = {0, 0, 0};
         if constexpr (sizeof(R) == 4) {
             run_pairs<R, RC, TWO_D, MIXED, 0>(std::make_integer_sequence<int, NP>{}, smem + cv.tile,
@@ -645,7 +655,7 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
                 dispatch_split<R, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, (uint32_t)tslot * 12u, FX, FY, tlen,
                                                        (uint32_t)tslot, hacc, nnv);
         }
-        const R hx = hacc[0][0] + hacc[1][0], hy = hacc[0][1] + hacc[1][1], hz = hacc[0][2] + hacc[1][2];
+        const R hx = sum_sets(hacc, 0), hy = sum_sets(hacc, 1), hz = sum_sets(hacc, 2);
         const long long site = ((long long)(w.x0 + cx + S * qx) * Y + (w.y0 + cy + S * qy)) * Z +
                                (TWO_D ? 0 : w.z0 + cz + S * qz);
         const R px = (R)gpx[site], py = (R)gpy[site], pz = (R)gpz[site];
