@@ -397,6 +397,9 @@ struct sn_handle {
     float dipole_ref = 0.0f;
     int rc = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host transfers overlapped with work on `stream`
+    static const int kSlabs = 8;
+    cudaEvent_t slab_ev[kSlabs] = {};
     std::vector<sn_replica_desc> desc;
     std::vector<SnTile> tiles;
     std::vector<SnReplicaDev> reps;
@@ -509,6 +512,20 @@ sn_status launch_field(sn_handle *h, int r, bool fp64, const SnFieldArgsHost &a)
     const bool two_d = h->desc[r].Z == 1;
     SN_CK(h, k_field[h->rc](fp64, two_d, h->mixed, &a, h->fwork_cnt[r], h->tiles[r].threads, h->tiles[r].field_smem,
                             h->stream));
+    h->launches++;
+    return SN_OK;
+}
+
+// Field pass over the blocks bx in [b0, b1) of replica r (the replica's block
+// list is x-major, so they are contiguous).
+sn_status launch_field_x(sn_handle *h, int r, const SnFieldArgsHost &base, int b0, int b1)
+{
+    if (b1 <= b0) return SN_OK;
+    const SnTile &t = h->tiles[r];
+    SnFieldArgsHost a = base;
+    a.work = base.work + (size_t)b0 * t.nb[1] * t.nb[2];
+    SN_CK(h, k_field[h->rc](false, h->desc[r].Z == 1, h->mixed, &a, (b1 - b0) * t.nb[1] * t.nb[2], t.threads,
+                            t.field_smem, h->stream));
     h->launches++;
     return SN_OK;
 }
@@ -649,6 +666,9 @@ void destroy_all(sn_handle *h)
                     h->d_aoff,  h->d_abins};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (auto &e : h->slab_ev)
+        if (e) cudaEventDestroy(e);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -877,8 +897,12 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         g_last_error = msg;
         return s;
     };
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(fail(h, SN_ERR_CUDA, "cudaStreamCreate failed"));
+    for (auto &e : h->slab_ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(h, SN_ERR_CUDA, "cudaEventCreate failed"));
 
     for (int r = 0; r < n_replicas; r++) {
         std::string why;
@@ -1029,20 +1053,51 @@ sn_status sn_gpu_upload_lattice(sn_handle *h, int replica, const float *xyz, con
     if (s) return s;
     if (!xyz) return fail(h, SN_ERR_ARG, "null xyz buffer");
     const SnReplicaDev &R = h->reps[replica];
+    const SnTile &t = h->tiles[replica];
     const size_t N = (size_t)R.n_sites;
     s = ensure(h, (void **)&h->d_stage, &h->stage_floats, 4 * N, sizeof(float));
     if (s) return s;
-    SN_CK(h, cudaMemcpyAsync(h->d_stage, xyz, 3 * N * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-    if (len) SN_CK(h, cudaMemcpyAsync(h->d_stage + 3 * N, len, N * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    // The copy runs in x slabs (whole block rows) on the copy stream; each slab
+    // is converted as soon as it lands, and the energy pass of the running
+    // total starts on every block whose tile (block + halo) has fully arrived,
+    // so the transfer and the recompute overlap.  Blocks whose halo wraps past
+    // x = 0 or X go last.
+    const int nb = t.nb[0], Bx = t.B[0], H = h->rc;
+    const int Q = std::max(1, std::min(sn_handle::kSlabs, nb));
+    const size_t row = (size_t)R.Y * R.Z;
+    double *red = h->d_red + 10 * replica;
     SN_CK(h, cudaMemsetAsync(h->d_flags, 0, 4 * sizeof(int), h->stream));
-    SN_CK(h, sn_launch_upload_convert(h->d_stage, len ? h->d_stage + 3 * N : nullptr, R.px, R.py, R.pz, R.len,
-                                      (long long)N, h->length, h->mixed ? 1 : 0, h->params.dipoles[0], h->d_flags,
-                                      h->stream));
+    SN_CK(h, cudaMemsetAsync(red, 0, 10 * sizeof(double), h->stream));
+    SN_CK(h, cudaEventRecord(h->slab_ev[0], h->stream));  // the copies must not overtake earlier work
+    SN_CK(h, cudaStreamWaitEvent(h->copy_stream, h->slab_ev[0], 0));
+    const SnFieldArgsHost fa = field_args(h, replica, nullptr, nullptr, h->d_red, 10);
+    int next_b = 1;  // block 0's tile wraps to the end of the lattice
+    for (int q = 0; q < Q; q++) {
+        const int x0 = (int)((long long)nb * q / Q) * Bx, x1 = (int)((long long)nb * (q + 1) / Q) * Bx;
+        const size_t a0 = (size_t)x0 * row, cnt = (size_t)(x1 - x0) * row;
+        SN_CK(h, cudaMemcpyAsync(h->d_stage + 3 * a0, xyz + 3 * a0, 3 * cnt * sizeof(float), cudaMemcpyHostToDevice,
+                                 h->copy_stream));
+        if (len)
+            SN_CK(h, cudaMemcpyAsync(h->d_stage + 3 * N + a0, len + a0, cnt * sizeof(float), cudaMemcpyHostToDevice,
+                                     h->copy_stream));
+        SN_CK(h, cudaEventRecord(h->slab_ev[q], h->copy_stream));
+        SN_CK(h, cudaStreamWaitEvent(h->stream, h->slab_ev[q], 0));
+        SN_CK(h, sn_launch_upload_convert(h->d_stage + 3 * a0, len ? h->d_stage + 3 * N + a0 : nullptr, R.px + a0,
+                                          R.py + a0, R.pz + a0, R.len + a0, (long long)cnt, h->length,
+                                          h->mixed ? 1 : 0, h->params.dipoles[0], h->d_flags, h->stream));
+        h->launches++;
+        // blocks whose tile x range [b*Bx - H, (b+1)*Bx + H) lies in [0, x1)
+        int last = (x1 - H) / Bx - 1;
+        if (q == Q - 1) last = nb - 1;
+        if ((s = launch_field_x(h, replica, fa, next_b, last + 1))) return s;
+        next_b = std::max(next_b, last + 1);
+    }
+    if ((s = launch_field_x(h, replica, fa, 0, 1))) return s;
+    SN_CK(h, sn_launch_recompute_finish(red, h->d_state, h->d_reps, replica, h->params.cage_strain, h->d_drift, 0,
+                                        h->stream));
     h->launches++;
     int flags[4] = {0, 0, 0, 0};
     SN_CK(h, cudaMemcpyAsync(flags, h->d_flags, sizeof(flags), cudaMemcpyDeviceToHost, h->stream));
-    s = recompute_one(h, replica, SN_ENERGY_FP32, 0);
-    if (s) return s;
     SN_CK(h, cudaStreamSynchronize(h->stream));
     if (flags[2]) return fail(h, SN_ERR_ARG, "negative or non-finite dipole length in upload");
     if (flags[0])
