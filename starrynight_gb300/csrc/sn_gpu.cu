@@ -71,8 +71,11 @@ struct SnPlan {
 int block_colour(const SnTile &t, const int *c) { return (c[0] % t.m[0]) * 4 + (c[1] % t.m[1]) * 2 + (c[2] % t.m[2]); }
 
 bool build_plan(const std::vector<SnTile> &tiles, const sn_replica_desc *replicas, int n, bool flow, SnPlan &pl,
-                std::string &why)
+                std::string &why, int ready = 512)
 {
+    // SN_FLOW_GROUP=W forces groups of W x slabs (-1: plain colour order); see below
+    int flow_group = 0;
+    if (const char *env = getenv("SN_FLOW_GROUP")) flow_group = atoi(env);
     std::vector<SnWork> &work = pl.work;
     for (int p = 0; p < 8; p++)
         for (int v = 0; v < 2; v++) {
@@ -108,14 +111,61 @@ bool build_plan(const std::vector<SnTile> &tiles, const sn_replica_desc *replica
     for (int v = 0; v < 2 && flow; v++) {
         pl.flow_off[v] = (int)work.size();
         std::unordered_map<uint64_t, int> index;  // (replica, block) -> position in this list
-        for (int p = 0; p < 8; p++) {
-            const int k = p * 2 + v;
-            for (int i = 0; i < pl.work_cnt[k]; i++) {
-                const SnWork w = work[pl.work_off[k] + i];
-                const SnTile &t = tiles[w.rep];
-                index[block_key(w.rep, w.x0 / t.B[0], w.y0 / t.B[1], w.z0 / t.B[2])] = (int)work.size() - pl.flow_off[v];
-                work.push_back(w);
+        // Queue order.  A replica whose block colours each hold at least
+        // `ready` blocks per group of W x slabs (block rows) is queued in such
+        // groups: the group's even slabs (block colours 0-3) in colour order,
+        // then the previous group's odd slabs (colours 4-7, which wait on even
+        // slabs of both groups), then the next group ...; the last group's odd
+        // slabs, which wait on slab 0 across the wrap, close its list.  Every
+        // block follows the blocks it waits on, enough blocks are ready at any
+        // time to fill the GPU, and the blocks in flight cover about two groups,
+        // so more halo re-reads hit L2.  Smaller replicas are queued together
+        // in plain colour order (colour 0 of all of them, then colour 1 ...).
+        // Within a colour: x, y, then z.
+        auto push_colour = [&](int r, int p, int bx0, int bx1) {
+            const SnTile &t = tiles[r];
+            const int cb[3] = {(p >> 2) & 1, (p >> 1) & 1, p & 1};
+            for (int bx = bx0; bx < bx1; bx++) {
+                if (bx % t.m[0] != cb[0]) continue;
+                for (int by = 0; by < t.nb[1]; by++)
+                    for (int bz = 0; bz < t.nb[2]; bz++) {
+                        if (by % t.m[1] != cb[1] || bz % t.m[2] != cb[2]) continue;
+                        index[block_key(r, bx, by, bz)] = (int)work.size() - pl.flow_off[v];
+                        work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
+                    }
             }
+        };
+        std::vector<int> small, large, width(n, 0);
+        for (int r = 0; r < n; r++) {
+            if ((replicas[r].Z == 1) != (v == 1)) continue;
+            const SnTile &t = tiles[r];
+            const int nbx = t.nb[0];
+            const long long per_slab = (long long)t.nb[1] * t.nb[2] / (t.m[1] * t.m[2]);  // one colour, one slab
+            int W = nbx;
+            if (t.m[0] == 2) {
+                if (flow_group > 0) {
+                    if (flow_group < nbx && nbx % flow_group == 0 && flow_group % 2 == 0) W = flow_group;
+                } else if (flow_group == 0) {
+                    for (int c = 2; c < nbx; c += 2)
+                        if (nbx % c == 0 && (long long)(c / 2) * per_slab >= ready) {
+                            W = c;
+                            break;
+                        }
+                }
+            }
+            width[r] = W;
+            (W == nbx ? small : large).push_back(r);
+        }
+        for (int p = 0; p < 8; p++)
+            for (int r : small) push_colour(r, p, 0, tiles[r].nb[0]);
+        for (int r : large) {
+            const int W = width[r], G = tiles[r].nb[0] / W;
+            for (int g = 0; g < G; g++) {
+                for (int p = 0; p < 4; p++) push_colour(r, p, g * W, (g + 1) * W);
+                if (g > 0)
+                    for (int p = 4; p < 8; p++) push_colour(r, p, (g - 1) * W, g * W);
+            }
+            for (int p = 4; p < 8; p++) push_colour(r, p, (G - 1) * W, G * W);
         }
         pl.flow_items[v] = (int)work.size() - pl.flow_off[v];
         deps.resize((size_t)(pl.flow_off[v] + pl.flow_items[v]) * SN_MAX_DEPS, 0);
@@ -940,7 +990,12 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     SnPlan plan;
     {
         std::string why;
-        if (!build_plan(h->tiles, replicas, n_replicas, h->flow, plan, why))
+        // blocks that must be ready at once to keep every CTA busy: ~1.5 per CTA slot at 2 CTAs per SM
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) !=
+                                                      cudaSuccess)
+            nsm = 0;
+        if (!build_plan(h->tiles, replicas, n_replicas, h->flow, plan, why, nsm > 0 ? 3 * nsm : 512))
             return bail(fail(h, SN_ERR_SCHEDULE, "%s", why.c_str()));
     }
     for (int k = 0; k < 16; k++) {
