@@ -448,7 +448,7 @@ struct sn_handle {
     int rc = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // host transfers overlapped with work on `stream`
-    static const int kSlabs = 8;
+    static constexpr int kSlabs = 8;
     cudaEvent_t slab_ev[kSlabs] = {};
     std::vector<sn_replica_desc> desc;
     std::vector<SnTile> tiles;
