@@ -513,72 +513,28 @@ __device__ __forceinline__ void st_release_gpu(uint32_t *p, uint32_t v)
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// L2 prefetch of the lattice rows a block's tile will copy (block + halo,
-// periodic wrap), one request per 128-byte line: issued for the CTA's next
-// block while it works on the current one, so that block's staging reads L2.
-template <int RC, bool TWO_D, bool MIXED>
-__device__ __forceinline__ void prefetch_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, int tid,
-                                              int nthreads)
-{
-    using G = Geo<RC, TWO_D>;
-    constexpr int H = G::H, HZ = G::HZ;
-    constexpr int NA = MIXED ? 4 : 3;  // px, py, pz (, len)
-    const int X = R.X, Y = R.Y, Z = R.Z;
-    const int Tx = Gm.T[0], Ty = Gm.T[1], Tz = Gm.T[2];
-    const int rows = Tx * Ty;
-    for (int i = tid; i < rows * NA; i += nthreads) {
-        const int arr = i / rows, r = i - (i / rows) * rows;
-        const int ux = r / Ty, uy = r - (r / Ty) * Ty;
-        const int gx = sn_wrap(w.x0 - H + ux, X), gy = sn_wrap(w.y0 - H + uy, Y);
-        const float *a = arr == 0 ? R.px : (arr == 1 ? R.py : (arr == 2 ? R.pz : R.len));
-        const float *row = a + ((long long)gx * Y + gy) * Z;
-        // z range [z0 - HZ, z0 - HZ + Tz), split where it wraps
-        int z0 = w.z0 - HZ, n = Tz;
-        if (z0 < 0) {
-            for (int z = Z + z0; z < Z; z += 32) asm volatile("prefetch.global.L2 [%0];" ::"l"(row + z));
-            n += z0;
-            z0 = 0;
-        }
-        const int zend = z0 + n;
-        const int zin = zend > Z ? Z : zend;
-        for (int z = z0; z < zin; z += 32) asm volatile("prefetch.global.L2 [%0];" ::"l"(row + z));
-        if (zin > z0) asm volatile("prefetch.global.L2 [%0];" ::"l"(row + zin - 1));
-        for (int z = 0; z < zend - Z; z += 32) asm volatile("prefetch.global.L2 [%0];" ::"l"(row + z));
-    }
-}
-
-// Dataflow sweep: one persistent launch for all blocks of one kernel variant
-// (the host sizes the grid with the occupancy API).  A CTA takes the queue's
-// next block, reserves the one after it (and prefetches that block's tile
-// into L2), waits until each adjacent block of an earlier colour has released
-// this sweep's done flag (a bounded spin; on time-out it records the error
-// for the host, which reports SN_ERR_TIMEOUT, and goes on), sweeps the block
-// and releases its own flag.  Adjacent blocks of later colours wait for this
-// one in turn, so every block sees exactly the lattice the colour-by-colour
-// order gives it.  Deadlock cannot occur: blocks only wait on blocks earlier
-// in the queue, and the earliest unfinished block any CTA holds is the one
-// that CTA is working on (a reserved block is later than its CTA's current
-// one), which waits on finished blocks only.
+// Dataflow sweep: one persistent launch per sweep.  Every CTA is resident
+// (the host sizes the grid with the occupancy API) and takes blocks from a
+// queue ordered by block colour.  Before updating a block it waits until
+// each adjacent block of an earlier colour has finished this sweep (a
+// bounded spin; on time-out it records SN_ERR_TIMEOUT in *err and goes on).
+// Adjacent blocks of later colours wait for this one in turn, so every block
+// sees exactly the lattice the phase-by-phase order gives it.  Deadlock
+// cannot occur: a block waited on was taken from the queue earlier by a CTA
+// that is running, and it only waits on blocks taken before it.
 template <int RC, bool TWO_D, bool MIXED>
 __global__ void __launch_bounds__(SN_SWEEP_MAX_THREADS, SN_SWEEP_MIN_BLOCKS) sweep_flow(const SnFlowArgs f)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_next;
+    __shared__ int s_item;
     const int tid = threadIdx.x;
     const uint32_t epoch = *f.base.sweep + 1u;
-    if (tid == 0) s_next = (int)atomicAdd(f.queue, 1u);
-    __syncthreads();
-    int item = s_next;
-    while (item < f.base.n_work) {
-        __syncthreads();  // every thread has read s_next
-        if (tid == 0) s_next = (int)atomicAdd(f.queue, 1u);
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(f.queue, 1u);
         __syncthreads();
-        const int next = s_next;
-        if (next < f.base.n_work) {
-            const SnWork wn = f.base.work[next];
-            const SnReplicaDev &Rn = f.base.reps[wn.rep];
-            prefetch_tile<RC, TWO_D, MIXED>(Rn, f.base.geoms[Rn.geom], wn, tid, blockDim.x);
-        }
+        const int item = s_item;
+        __syncthreads();
+        if (item >= f.base.n_work) break;
         const int *dl = f.deps + (size_t)item * SN_MAX_DEPS;
         if (tid < dl[0]) {
             const uint32_t *flag = f.done + dl[1 + tid];
@@ -603,7 +559,6 @@ __global__ void __launch_bounds__(SN_SWEEP_MAX_THREADS, SN_SWEEP_MIN_BLOCKS) swe
             __threadfence();
             st_release_gpu(f.done + item, epoch);
         }
-        item = next;
     }
 }
 
