@@ -117,3 +117,32 @@ def test_replica_table_64_uneven_with_exchange(native_lib):
     assert 0 < ok <= att
     np.testing.assert_allclose(np.sort(temps), np.sort(T.astype(np.float32)), rtol=1e-6)
     assert np.all(np.abs(E_run - E_chk) <= 1e-7 * np.abs(E_chk) + 1e-6)
+
+
+def test_largest_lattice_512cubed(native_lib):
+    """512^3 (134 M sites, 2.1 GB): the running energy after two sweeps equals a fresh
+    FP32-field recompute and the all-FP64 pass, and every occupied site is attempted once."""
+    sn = native_lib
+    params = sn.ModelParams(cutoff=3, efield=(0.0, 0.0, 0.1), dipoles=(1.0, 0.0), prevalence=(0.7, 0.3), seed=51)
+    with sn.Simulation(params, [sn.Replica(512, 512, 512, T=150.0, seed=51)]) as sim:
+        sim.init_lattice(0)
+        sim.set_recompute(0)
+        acc, rej = sim.sweep(2, counts=True)
+        E_run = sim.observables()["E_per_site"][0] * 512 ** 3
+        E32 = sim.energy(0, "fp32")
+        E64 = sim.energy(0, "fp64")
+        _, ln = sim.download(0)
+    occ = int((ln > 0).sum())
+    assert acc + rej == 2 * occ
+    assert 0 < acc < acc + rej
+    assert abs(E_run - E64) <= 1e-8 * abs(E64)
+    assert abs(E32 - E64) <= 1e-7 * abs(E64)
+
+
+def test_oversized_lattices_are_refused(native_lib):
+    """More than 2^31 - 1 sites, or a side above 32767, is an argument error before any allocation."""
+    sn = native_lib
+    params = sn.ModelParams(cutoff=3)
+    for shape in ((1300, 1300, 1300), (32768, 2, 2)):
+        with pytest.raises(sn.SnError):
+            sn.Simulation(params, [sn.Replica(*shape)])

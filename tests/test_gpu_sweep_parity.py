@@ -28,6 +28,8 @@ CASES = [
     ("circle_dim2", (8, 8, 8), 3, 300.0, (0, 0, 0), 0.0, 1.0, (1.0,), (1.0,), False, 2, 3),
     ("mixture", (12, 12, 12), 3, 300.0, (0, 0, 0.1), 0.0, 1.0, (1.0, 0.5, 0.0), (0.5, 0.3, 0.2), False, 3, 3),
     ("length2", (8, 8, 8), 3, 300.0, (0, 0, 0), 0.0, 1.0, (2.0,), (1.0,), False, 3, 3),
+    ("rc1", (8, 12, 8), 1, 300.0, (0.0, 0.1, 0.0), 0.0, 1.0, (1.0, 0.0), (0.8, 0.2), False, 3, 3),
+    ("rc6", (24, 24, 24), 6, 300.0, (0.0, 0.0, 0.1), 0.0, 1.0, (1.0,), (1.0,), False, 3, 2),
 ]
 
 
