@@ -112,7 +112,10 @@ def test_running_total_has_no_drift(native_lib):
 def test_adjoint_matches_fp64_gradient_and_finite_differences(native_lib):
     """Config-4 parameters on a 20^3 lattice: dE/dp_i against the analytic FP64
     gradient and central FP64 finite differences (h = 1e-4) on 256 random
-    sites, and dE/d(Dipole, CageStrain, Efield) against finite differences."""
+    sites -- through the oracle's site energy change (the restatement of the
+    reference's site_energy, pinned to its golden values), which is exactly
+    E(p') - E(p) -- and on 4 sites through the full FP64 total energy, and
+    dE/d(Dipole, CageStrain, Efield) against finite differences."""
     sn = native_lib
     shape = (20, 20, 20)
     kw = dict(cutoff=4, cage_strain=0.5, efield=(0.05, 0.0, 0.05), dipoles=(1.0, 0.0), prevalence=(0.9, 0.1))
@@ -134,7 +137,19 @@ def test_adjoint_matches_fp64_gradient_and_finite_differences(native_lib):
     rng = np.random.default_rng(7)
     h = 1e-4
     sites = rng.choice(np.nonzero(ln)[0], 256, replace=False)
+    # central finite differences of the FP64 total energy; only site i changes, so
+    # E(p_i + h e_k) - E(p_i - h e_k) is the difference of the two local FP64 changes
     for i in sites:
+        for k in range(3):
+            up, dn = xyz[i].copy(), xyz[i].copy()
+            up[k] = xyz[i, k] + np.float32(h)
+            dn[k] = xyz[i, k] - np.float32(h)
+            ep = O.delta_energy64(m, px, py, pz, ln, int(i), up)
+            em = O.delta_energy64(m, px, py, pz, ln, int(i), dn)
+            fd = (ep - em) / (float(up[k]) - float(dn[k]))
+            assert abs(g[i, k] - fd) <= 1e-4 * max(1.0, abs(fd)), (i, k, g[i, k], fd)
+    # and a few through the full FP64 energy itself
+    for i in sites[:4]:
         for k, arr in enumerate((px, py, pz)):
             o = arr[i]
             arr[i] = o + np.float32(h)
