@@ -93,10 +93,6 @@ typedef struct sn_schedule_info {
     int smem_bytes;        /* dynamic shared memory per block           */
     int merge;             /* 1: colour pairs c, c + (s/2,s/2,s/2)      */
     int threads;           /* threads per block of the sweep kernel     */
-    int row_stride;        /* tile slots between adjacent y rows        */
-    int plane_stride;      /* tile slots between adjacent x planes      */
-    int tile_offset;       /* slot of tile site (0,0,0)                 */
-    int vec_stage;         /* 1: 16-byte staging of z rows              */
 } sn_schedule_info;
 
 /* Initial lattice patterns (InitialLattice, src/starrynight-main.c:184-203). */

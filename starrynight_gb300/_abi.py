@@ -49,8 +49,7 @@ class ReplicaDesc(ctypes.Structure):
 
 class ScheduleInfo(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in ("bx", "by", "bz", "nbx", "nby", "nbz", "mx", "my", "mz", "s",
-                                             "halo", "tile_slots", "smem_bytes", "merge", "threads",
-                                             "row_stride", "plane_stride", "tile_offset", "vec_stage")]
+                                             "halo", "tile_slots", "smem_bytes", "merge", "threads")]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -361,31 +361,17 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
             t.ng = ng;
             t.merge = merge;
             if (t.threads > (pass == 0 ? SN_TWO_PER_SM_THREADS : SN_SWEEP_MAX_THREADS)) continue;
-            // 16-byte staging of z rows: needs whole 4-site chunks in every row
-            // (Z and the block's z extent multiples of 4, so each row starts a
-            // fixed a = (-halo) mod 4 sites after an aligned chunk) and row
-            // and plane strides that keep those chunks 16-byte aligned in the
-            // tile, with room for the a-site overhang before each row and the
-            // rounding after it.  The tile is shifted by a slots for that.
-            t.vec = (!two_d && Z % 4 == 0 && c.B[2] % 4 == 0) ? 1 : 0;
-            const int va = t.vec ? (4 - rc % 4) % 4 : 0;
-            const int vrow = t.vec ? ((t.T[2] + va + 3) / 4) * 4 - va : 0;  // slots a row's chunks reach past its start
-            t.off0 = va;
-            const int vextra = t.vec ? va + 4 : 0;
             const int pc_min = pass == 0 ? std::min(8, ng) : 1;
             // quick lower bound on shared memory with no padding
-            if ((int)sn_sweep::sn_carve(t.T[0] * t.T[1] * t.T[2] + vextra, t.tg, pc_min, NS, S, NF, mixed, 4).total >
-                limit)
+            if ((int)sn_sweep::sn_carve(t.T[0] * t.T[1] * t.T[2], t.tg, pc_min, NS, S, NF, mixed, 4).total > limit)
                 continue;
             long long best = -1;
             int bSy = 0, bSx = 0;
             for (int dy = 0; dy < 32; dy++) {
                 const int Sy = t.T[2] + dy;
-                if (t.vec && (Sy % 4 || Sy < vrow)) continue;
                 for (int dx = 0; dx < 32; dx++) {
                     const int Sx = t.T[1] * Sy + dx;
-                    if (t.vec && Sx % 4) continue;
-                    if ((int)sn_sweep::sn_carve(Sx * t.T[0] + vextra, t.tg, pc_min, NS, S, NF, mixed, 4).total > limit)
+                    if ((int)sn_sweep::sn_carve(Sx * t.T[0], t.tg, pc_min, NS, S, NF, mixed, 4).total > limit)
                         continue;
                     const long long cost = conflict_cost(t, S, two_d, Sy, Sx);
                     if (best < 0 || cost < best) {
@@ -398,7 +384,7 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
             if (best < 0) continue;
             t.Sy = bSy;
             t.Sx = bSx;
-            t.slots = bSx * t.T[0] + vextra;
+            t.slots = bSx * t.T[0];
             // stage as many groups' proposals at once as the budget allows
             t.pc = ng;
             while (t.pc > 1 && (int)sn_sweep::sn_carve(t.slots, t.tg, t.pc, NS, S, NF, mixed, 4).total > limit) t.pc--;
@@ -430,10 +416,6 @@ void fill_info(const SnTile &t, int rc, sn_schedule_info *o)
     o->smem_bytes = t.smem_bytes;
     o->merge = t.merge;
     o->threads = t.threads;
-    o->row_stride = t.Sy;
-    o->plane_stride = t.Sx;
-    o->tile_offset = t.off0;
-    o->vec_stage = t.vec;
 }
 
 }  // namespace

@@ -51,8 +51,6 @@ struct SnTile {
     int start[3][SN_MAX_S];
     int smem_bytes;  // dynamic shared memory for the sweep kernel
     int field_smem;  // dynamic shared memory for the field kernel
-    int vec;         // 1: tiles are staged 16 bytes (4 z sites) at a time
-    int off0;        // slot of tile site (0,0,0); slots 0..off0-1 take the alignment overhang
 };
 
 struct SnReplicaDev {

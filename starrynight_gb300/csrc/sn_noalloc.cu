@@ -25,7 +25,6 @@
 // The first call on each device looks up the array's device address with
 // cudaGetSymbolAddress (with that device current) and caches it; make that
 // first call before any stream capture begins.
-#include <cstdint>
 #include <cstdio>
 #include <cstring>
 
@@ -101,8 +100,6 @@ sn_status sn_gpu_energy_noalloc(const float *d_px, const float *d_py, const floa
     SnTile tile;
     char why[200];
     if (!sn_internal_plan(X, Y, Z, P.cutoff, mixed, &tile, why, sizeof(why))) return nfail(SN_ERR_SCHEDULE, why);
-    // 16-byte tile staging reads the caller's arrays four sites at a time: only when they allow it
-    if (((uintptr_t)d_px | (uintptr_t)d_py | (uintptr_t)d_pz | (uintptr_t)d_len) & 15u) tile.vec = 0;
     const long long nblocks = (long long)tile.nb[0] * tile.nb[1] * tile.nb[2];
     if (nblocks > SN_NOALLOC_MAX_BLOCKS) {
         snprintf(g_err, sizeof(g_err),

@@ -282,34 +282,6 @@ __device__ __forceinline__ void stage_tile(const SnReplicaDev &R, const SnTile &
     const int lane = tid & 31, warp = tid >> 5, nwarps = nthreads >> 5;
     const int X = R.X, Y = R.Y, Z = R.Z;
     const int Tx = Gm.T[0], Ty = Gm.T[1], Tz = Gm.T[2];
-    if (!TWO_D && Gm.vec) {
-        // 16 bytes at a time: thread takes chunk k (4 z sites) of one tile row,
-        // loads it from px, py, pz (and len) and stores the 12 interleaved
-        // floats as three 16-byte words.  Chunks start a = off0 sites before
-        // the row, at 16-byte boundaries in both the lattice and the tile
-        // (the planner's strides guarantee it); z wraps chunk by chunk.
-        const int a = Gm.off0;
-        const int nch = (Tz + a + 3) >> 2;
-        for (int it = tid; it < Tx * Ty * nch; it += nthreads) {
-            const int row = it / nch, k = it - (it / nch) * nch;
-            const int ux = row / Ty, uy = row - (row / Ty) * Ty;
-            const int gx = sn_wrap(w.x0 - H + ux, X), gy = sn_wrap(w.y0 - H + uy, Y);
-            int zc = w.z0 - HZ - a + 4 * k;
-            zc = zc < 0 ? zc + Z : (zc >= Z ? zc - Z : zc);
-            const long long g = ((long long)gx * Y + gy) * Z + zc;
-            const int slot = sn_pi<S>(start, ux) * Gm.Sx + sn_pi<S>(start + SN_MAX_S, uy) * Gm.Sy - a + 4 * k;
-            const float4 vx = __ldcg(reinterpret_cast<const float4 *>(R.px + g));
-            const float4 vy = __ldcg(reinterpret_cast<const float4 *>(R.py + g));
-            const float4 vz = __ldcg(reinterpret_cast<const float4 *>(R.pz + g));
-            float4 *d = reinterpret_cast<float4 *>(tile + 3 * slot);
-            d[0] = make_float4(vx.x, vy.x, vz.x, vx.y);
-            d[1] = make_float4(vy.y, vz.y, vx.z, vy.z);
-            d[2] = make_float4(vz.z, vx.w, vy.w, vz.w);
-            if constexpr (MIXED)
-                *reinterpret_cast<float4 *>(tlen + slot) = __ldcg(reinterpret_cast<const float4 *>(R.len + g));
-        }
-        return;
-    }
     for (int row = warp; row < Tx * Ty; row += nwarps) {
         const int ux = row / Ty, uy = row - (row / Ty) * Ty;
         const int gx = sn_wrap(w.x0 - H + ux, X), gy = sn_wrap(w.y0 - H + uy, Y);
@@ -361,9 +333,8 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
     const float Lu = R.length;
 
     const Carve cv = sn_carve(Gm.slots, tg, pc, NS, S, NF, MIXED, 4);
-    unsigned char *tbase = smem + cv.tile + 12 * Gm.off0;  // slot 0 = tile site (0,0,0)
-    float *tile = reinterpret_cast<float *>(tbase);
-    float *tlen = reinterpret_cast<float *>(smem + cv.tlen) + Gm.off0;
+    float *tile = reinterpret_cast<float *>(smem + cv.tile);
+    float *tlen = reinterpret_cast<float *>(smem + cv.tlen);
     float4 *props = reinterpret_cast<float4 *>(smem + cv.props);
     float *parts = reinterpret_cast<float *>(smem + cv.parts);
     int *ftab = reinterpret_cast<int *>(smem + cv.ftab);
@@ -455,7 +426,7 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
         if (active) {
             float hacc[SN_ACC_SETS][3] = {};
             float nn[3] = {0.f, 0.f, 0.f};
-            dispatch_split<float, RC, TWO_D, MIXED, 0>(j, tbase, (uint32_t)tslot * 12u, FX, FY, tlen,
+            dispatch_split<float, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, (uint32_t)tslot * 12u, FX, FY, tlen,
                                                        (uint32_t)tslot, hacc, nn);
             const float sc = MIXED ? tlen[tslot] : Lu * Lu;
             float *pp = parts + (j * 3) * tg + tt;
@@ -639,14 +610,13 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
     const R Lu = (R)Rp.length;
 
     const Carve cv = sn_carve(Gm.slots, tg, 0, G::NS, S, NF, MIXED, (int)sizeof(R));
-    unsigned char *tbase = smem + cv.tile + 12 * Gm.off0;  // slot 0 = tile site (0,0,0)
-    float *tlen = reinterpret_cast<float *>(smem + cv.tlen) + Gm.off0;
+    float *tlen = reinterpret_cast<float *>(smem + cv.tlen);
     int *ftab = reinterpret_cast<int *>(smem + cv.ftab);
     int *start = reinterpret_cast<int *>(smem + cv.start);
     double *red = reinterpret_cast<double *>(smem + cv.red);
 
     build_tables<RC, TWO_D>(Gm, start, ftab, tid, nthreads);
-    stage_tile<RC, TWO_D, MIXED>(Rp, Gm, w, reinterpret_cast<float *>(tbase), tlen, start, tid, nthreads);
+    stage_tile<RC, TWO_D, MIXED>(Rp, Gm, w, reinterpret_cast<float *>(smem + cv.tile), tlen, start, tid, nthreads);
     cp_async_wait_all();
     __syncthreads();
 
@@ -676,13 +646,13 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
         R hacc[SN_ACC_SETS][3] = {};
         R nnv[3] = {0, 0, 0};
         if constexpr (sizeof(R) == 4) {
-            run_pairs<R, RC, TWO_D, MIXED, 0>(std::make_integer_sequence<int, NP>{}, tbase,
+            run_pairs<R, RC, TWO_D, MIXED, 0>(std::make_integer_sequence<int, NP>{}, smem + cv.tile,
                                               (uint32_t)tslot * 12u, FX, FY, tlen, (uint32_t)tslot, hacc, nnv);
         } else {
             // FP64 validation mode: one stencil slice at a time keeps the double registers in check
 #pragma unroll 1
             for (int j = 0; j < G::NS; j++)
-                dispatch_split<R, RC, TWO_D, MIXED, 0>(j, tbase, (uint32_t)tslot * 12u, FX, FY, tlen,
+                dispatch_split<R, RC, TWO_D, MIXED, 0>(j, smem + cv.tile, (uint32_t)tslot * 12u, FX, FY, tlen,
                                                        (uint32_t)tslot, hacc, nnv);
         }
         const R hx = sum_sets(hacc, 0), hy = sum_sets(hacc, 1), hz = sum_sets(hacc, 2);
