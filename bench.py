@@ -329,6 +329,7 @@ def run_ours(args, ws, rank, local):
     total_upd = dist_sum(ws, float(occ) * args.steps)
     value = total_upd / (ms * 1e-3)
     drift, nchk = sim.drift()
+    acc_n, rej_n = sim.sweep(5, counts=True)  # acceptance ratio, outside the timed region
     # accuracy: running total vs a full FP64 recompute, FP32-field site energies vs FP64
     obs = sim.observables()
     E_run = obs["E_per_site"][0] * N
@@ -337,7 +338,8 @@ def run_ours(args, ws, rank, local):
     occm = ln > 0
     err = np.abs(site32[occm] - site64[occm])
     rel = err / np.maximum(np.abs(site64[occm]), 1.0)
-    acc_info = {"running_vs_fp64_rel": abs(E_run - E64) / abs(E64), "max_drift_fp32_checks": drift,
+    acc_info = {"acceptance_ratio": acc_n / max(1, acc_n + rej_n),
+                "running_vs_fp64_rel": abs(E_run - E64) / abs(E64), "max_drift_fp32_checks": drift,
                 "site_energy_rel_err_max": float(rel.max()), "site_energy_rel_err_mean": float(rel.mean()),
                 "site_energy_abs_err_max": float(err.max()),
                 "site_energy_rel_floor": 1.0,
