@@ -1,8 +1,9 @@
 // sn_gpu.cu -- host implementation of the C ABI in include/sn_gpu.h.
 //
 // One handle = one replica table resident in HBM + one CUDA stream.  A sweep
-// is captured once as a CUDA graph (8 block-colour launches of the sweep
-// kernel + the end-of-sweep fold) and replayed; every per-sweep quantity the
+// is captured once as a CUDA graph (one dataflow launch of the sweep kernel
+// per kernel variant -- or, with SN_SCHEDULE=phases, 8 block-colour launches
+// -- plus the end-of-sweep fold) and replayed; every per-sweep quantity the
 // kernels need (sweep index, temperatures, fields) lives in device memory so
 // the graph never changes.
 #include <algorithm>

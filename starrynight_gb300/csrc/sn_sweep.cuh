@@ -1,12 +1,13 @@
-// sn_sweep.cuh -- the Metropolis sweep kernel (one block colour per launch).
+// sn_sweep.cuh -- the Metropolis sweep kernels and the field (energy) pass.
 //
 // Schedule.  A replica's lattice is cut into blocks of B = (bx,by,bz) sites;
-// blocks get a checkerboard colour (block index mod 2 per axis).  One launch
-// handles every block of one block colour, one CTA per block.  Two blocks of
-// the same colour are at least one block (>= cutoff sites) apart, so they
-// never interact and their CTAs run independently; each CTA reads its halo
-// (cutoff sites around the block) from blocks of other colours, which no
-// CTA of this launch writes.  Inside the block the CTA visits the s^3 site
+// blocks get a checkerboard colour (block index mod 2 per axis).  Blocks of
+// one colour never interact (two of them are at least one block, >= cutoff
+// sites, apart); a block's halo (cutoff sites around it) lies in blocks of
+// other colours.  sweep_phase runs one launch per block colour, one CTA per
+// block; sweep_flow runs a whole sweep as one persistent launch in which a
+// block waits only for its adjacent blocks of earlier colours -- the same
+// reads and writes for every block.  Inside the block the CTA visits the s^3 site
 // colours (local coordinate mod s, s = cutoff + 1) in order; sites of one
 // site colour are >= s apart and are updated together.  Every occupied site
 // is attempted exactly once per sweep: the same set of moves as MC_moves
