@@ -362,7 +362,7 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
             t.ng = ng;
             t.merge = merge;
             if (t.threads > (pass == 0 ? SN_TWO_PER_SM_THREADS : SN_SWEEP_MAX_THREADS)) continue;
-            const int pc_min = 2;  // proposals double-buffered by colour group
+            const int pc_min = pass == 0 ? std::min(8, ng) : 1;
             // quick lower bound on shared memory with no padding
             if ((int)sn_sweep::sn_carve(t.T[0] * t.T[1] * t.T[2], t.tg, pc_min, NS, S, NF, mixed, 4).total > limit)
                 continue;
@@ -386,7 +386,9 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
             t.Sy = bSy;
             t.Sx = bSx;
             t.slots = bSx * t.T[0];
-            t.pc = 2;
+            // stage as many groups' proposals at once as the budget allows
+            t.pc = ng;
+            while (t.pc > 1 && (int)sn_sweep::sn_carve(t.slots, t.tg, t.pc, NS, S, NF, mixed, 4).total > limit) t.pc--;
             t.smem_bytes = (int)sn_sweep::sn_carve(t.slots, t.tg, t.pc, NS, S, NF, mixed, 4).total;
             t.field_smem = (int)sn_sweep::sn_carve(t.slots, t.tg, 0, NS, S, NF, mixed, 8).total;
             if (t.smem_bytes > limit || t.field_smem > kSmemLimit || t.pc < pc_min) continue;

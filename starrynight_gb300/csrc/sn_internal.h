@@ -45,7 +45,7 @@ struct SnTile {
     int tp;          // targets of one site colour, padded to a warp multiple
     int tg;          // targets of one colour group (1 or 2 colours)
     int ng;          // colour groups per block
-    int pc;          // colour groups whose proposals are held at once (2: double buffer)
+    int pc;          // colour groups whose proposals are staged at once
     int threads;     // sweep / field kernel block size (splits * tg)
     int merge;       // 1: colours c and c + (s/2,s/2,s/2) are updated together
     int start[3][SN_MAX_S];

@@ -360,6 +360,7 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
 
     int FX[NF], FY[NF];
     int pcx = -1, pcy = -1;
+    int gchunk = 0, gnext = 0;  // first group of the staged chunk, first group of the next
     // groups in which this thread's target exists (bit g), computed once
     unsigned long long amask = 0ull;
     for (int g = 0; g < ng && g < 64; g++) {
@@ -368,40 +369,42 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
         if (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) && (TWO_D || qz < sn_count(Bz, cz, S)))
             amask |= 1ull << g;
     }
-    // Proposal and accept threshold for target tq of group gq: (p', -ln(u)/beta),
-    // w = -1 at a vacancy, -2 where the colour has no such target.
-    auto draw = [&](int gq, int tq) -> float4 {
-        const int h2 = tq / tp, t2 = tq - (tq / tp) * tp;
-        const int qz2 = t2 % nqz, qy2 = (t2 / nqz) % nqy, qx2 = t2 / (nqz * nqy);
-        int cx, cy, cz;
-        group_colour<S, SZ, MERGE>(gq, h2, cx, cy, cz);
-        float4 pr = make_float4(0.0f, 0.0f, 0.0f, -2.0f);
-        if (qx2 < Gm.nq[0] && qx2 < sn_count(Bx, cx, S) && qy2 < sn_count(By, cy, S) &&
-            (TWO_D || qz2 < sn_count(Bz, cz, S))) {
-            const int site = ((w.x0 + cx + S * qx2) * Y + (w.y0 + cy + S * qy2)) * Z +
-                             (TWO_D ? 0 : w.z0 + cz + S * qz2);
-            pr.w = -1.0f;  // vacancy
-            if (glen[site] != 0.0f) {
-                float3 p;
-                float u;
-                if (!sn_proposal((uint32_t)site, sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
-                    p = make_float3(FLOW ? __ldcg(gpx + site) : gpx[site], FLOW ? __ldcg(gpy + site) : gpy[site],
-                                    FLOW ? __ldcg(gpz + site) : gpz[site]);
-                // accept iff dE < -ln(u)/beta  <=>  dE < 0 || exp(-beta dE) > u
-                const float thr = u > 0.0f ? -logf(u) / beta : INFINITY;
-                pr = make_float4(p.x, p.y, p.z, thr);
-            }
-        }
-        return pr;
-    };
-    // Proposals are double-buffered by group: group 0's are drawn while the
-    // tile arrives; group g+1's are drawn by the split j = 1 threads while the
-    // split j = 0 threads finalize group g (with one split, by the finalizing
-    // threads after their finalize).
-    if (tid < tg) props[tid] = draw(0, tid);
-    cp_async_wait_all();
-    __syncthreads();
     for (int g = 0; g < ng; g++) {
+        // ---- proposals and accept thresholds of the next pc groups ------------
+        // Thread (j, tt) draws for its own target tt in groups g0+j, g0+j+NS, ...
+        if (g == gnext) {
+            __syncthreads();  // previous chunk fully consumed
+            gchunk = g;
+            gnext = min(g + pc, ng);
+            if (tid < NS * tg) {
+                for (int k = j; k < gnext - g; k += NS) {
+                    int cx, cy, cz;
+                    group_colour<S, SZ, MERGE>(g + k, hh, cx, cy, cz);
+                    float4 pr = make_float4(0.0f, 0.0f, 0.0f, -2.0f);  // no target here
+                    if ((g + k < 64) ? ((amask >> (g + k)) & 1ull)
+                                     : (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
+                                        (TWO_D || qz < sn_count(Bz, cz, S)))) {
+                        const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + (TWO_D ? 0 : w.z0 + cz) + srel;
+                        pr.w = -1.0f;  // vacancy
+                        if (glen[site] != 0.0f) {
+                            float3 p;
+                            float u;
+                            if (!sn_proposal((uint32_t)site, sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
+                                p = make_float3(FLOW ? __ldcg(gpx + site) : gpx[site],
+                                                FLOW ? __ldcg(gpy + site) : gpy[site],
+                                                FLOW ? __ldcg(gpz + site) : gpz[site]);
+                            // accept iff dE < -ln(u)/beta  <=>  dE < 0 || exp(-beta dE) > u
+                            const float thr = u > 0.0f ? -logf(u) / beta : INFINITY;
+                            pr = make_float4(p.x, p.y, p.z, thr);
+                        }
+                    }
+                    props[k * tg + tt] = pr;
+                }
+            }
+            if (g == 0) cp_async_wait_all();
+            __syncthreads();
+        }
+
         int cx, cy, cz;
         group_colour<S, SZ, MERGE>(g, hh, cx, cy, cz);
         const bool active = (g < 64) ? ((amask >> g) & 1ull) != 0ull
@@ -436,7 +439,7 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
 
         // ---- 2. finalize: dE, accept, update ------------------------------------------
         if (j == 0 && active) {
-            const float4 pr = props[(g & 1) * tg + tt];
+            const float4 pr = props[(g - gchunk) * tg + tt];
             if (pr.w >= 0.0f) {
                 float gx = Ex, gy = Ey, gz = Ez;
 #pragma unroll
@@ -466,14 +469,6 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
                     sPy.add(Li * dy);
                     sPz.add(Li * dz);
                 }
-            }
-        }
-        // ---- 3. proposals of the next group, meanwhile ---------------------------------
-        if (g + 1 < ng) {
-            if constexpr (NS > 1) {
-                if (j == 1) props[((g + 1) & 1) * tg + tt] = draw(g + 1, tt);
-            } else {
-                if (tid < tg) props[((g + 1) & 1) * tg + tid] = draw(g + 1, tid);
             }
         }
         __syncthreads();
