@@ -70,6 +70,8 @@ typedef struct sn_replica_desc {
     int has_efield;        /* 1: efield below replaces sn_params.efield    */
     float efield[3];
     uint64_t seed;         /* Philox key of this replica; 0 -> params.seed + replica */
+    int block[3];          /* block shape to use (from sn_plan_candidates or a
+                              tuner); 0,0,0 -> the planner's first choice     */
 } sn_replica_desc;
 
 /* The block/colour schedule chosen for one replica (what the CPU oracle
@@ -278,6 +280,12 @@ sn_status sn_gpu_proposals(const sn_handle *h, int replica, const uint32_t *site
 sn_status sn_gpu_schedule(const sn_handle *h, int replica, sn_schedule_info *out);
 /* Host-only: the schedule sn_gpu_init would pick (no GPU needed). */
 sn_status sn_plan_schedule(int X, int Y, int Z, int cutoff, int mixed_lengths, sn_schedule_info *out);
+/* Host-only: up to max_out feasible schedules in the planner's order of
+ * preference (the first is sn_plan_schedule's); *n_out receives the count.
+ * An autotuner times them and passes the winner's block shape in
+ * sn_replica_desc.block. */
+sn_status sn_plan_candidates(int X, int Y, int Z, int cutoff, int mixed_lengths, sn_schedule_info *out,
+                             int max_out, int *n_out);
 /* Host-only: 1 if no two sites updated together interact under periodic
  * boundaries (same block colour and site colour within the cutoff). */
 int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *sched);

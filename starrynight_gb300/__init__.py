@@ -8,9 +8,9 @@ raises.
 from .native import build, lib_path, driver_path
 from ._abi import SnError
 from .sim import (ModelParams, Replica, Simulation, check_flow, check_schedule, fp32_peak, neighbour_count, philox,
-                  plan_schedule)
+                  plan_candidates, plan_schedule)
 
 __all__ = [
     "build", "lib_path", "driver_path", "SnError", "ModelParams", "Replica", "Simulation",
-    "check_flow", "check_schedule", "fp32_peak", "neighbour_count", "philox", "plan_schedule",
+    "check_flow", "check_schedule", "fp32_peak", "neighbour_count", "philox", "plan_candidates", "plan_schedule",
 ]

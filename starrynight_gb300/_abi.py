@@ -44,6 +44,7 @@ class ReplicaDesc(ctypes.Structure):
     _fields_ = [
         ("X", ctypes.c_int), ("Y", ctypes.c_int), ("Z", ctypes.c_int), ("T", ctypes.c_float),
         ("has_efield", ctypes.c_int), ("efield", ctypes.c_float * 3), ("seed", ctypes.c_uint64),
+        ("block", ctypes.c_int * 3),
     ]
 
 
@@ -102,6 +103,7 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_quench": ([h, _i, _i, ctypes.c_float, _vp], _i),
             "sn_gpu_schedule": ([h, _i, _P(ScheduleInfo)], _i),
             "sn_plan_schedule": ([_i, _i, _i, _i, _i, _P(ScheduleInfo)], _i),
+            "sn_plan_candidates": ([_i, _i, _i, _i, _i, _P(ScheduleInfo), _i, _P(_i)], _i),
             "sn_check_schedule": ([_i, _i, _i, _i, _P(ScheduleInfo)], _i),
             "sn_check_flow": ([_P(Params), _i, _P(ReplicaDesc), _vp], _i),
             "sn_gpu_launch_count": ([h, _P(ctypes.c_uint64)], _i),

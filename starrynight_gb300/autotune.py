@@ -1,0 +1,53 @@
+"""Empirical tile/colour-schedule autotuner.
+
+The planner (``plan_candidates``) ranks the feasible block shapes of a
+lattice by a model -- largest blocks that fit two CTAs per SM, least halo,
+conflict-free shared-memory strides.  ``tune`` times the top candidates on
+the GPU (CUDA events around whole sweeps, after warm-up) and returns the
+fastest shape; ``tune_table`` does so once per distinct lattice size of a
+replica table and returns the table with every replica's ``block`` set.
+
+A block shape changes the order in which sites are updated (every shape is
+an exact Metropolis sweep, so the physics is the same but trajectories
+differ); the tuned shape is a per-lattice-size choice a run keeps fixed.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Sequence
+
+from .sim import ModelParams, Replica, Simulation, plan_candidates
+
+
+def _mixed(params: ModelParams) -> bool:
+    return len({float(d) for d in params.dipoles if float(d) > 0.0}) > 1
+
+
+def tune(params: ModelParams, replica: Replica, max_candidates: int = 6, sweeps: int = 5,
+         warmup: int = 2) -> tuple:
+    """(best (bx, by, bz), [(shape, ms per sweep), ...]) for one lattice size."""
+    cands = plan_candidates(replica.X, replica.Y, replica.Z, params.cutoff, _mixed(params), max_candidates)
+    results = []
+    for c in cands:
+        shape = (c["bx"], c["by"], c["bz"])
+        rep = dataclasses.replace(replica, block=shape)
+        with Simulation(params, [rep]) as sim:
+            sim.init_lattice(0)
+            sim.set_recompute(0)
+            sim.sweep(warmup)
+            _, ms, _ = sim.phase_times(sweeps)
+        results.append((shape, ms))
+    best = min(results, key=lambda r: r[1])[0]
+    return best, results
+
+
+def tune_table(params: ModelParams, replicas: Sequence[Replica], **kw) -> list:
+    """The table with each replica's block shape tuned (once per distinct size)."""
+    chosen = {}
+    out = []
+    for r in replicas:
+        key = (r.X, r.Y, r.Z)
+        if key not in chosen:
+            chosen[key] = tune(params, r, **kw)[0]
+        out.append(dataclasses.replace(r, block=chosen[key]))
+    return out

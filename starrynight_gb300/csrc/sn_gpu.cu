@@ -283,7 +283,10 @@ std::vector<int> block_candidates(int L, int rc)
     return c;
 }
 
-bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string &why)
+// Feasible tile plans of an X x Y x Z replica in preference order (at most
+// max_out; force = a block shape to use instead of choosing).
+bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &outs, size_t max_out, std::string &why,
+                const int *force_shape = nullptr)
 {
     if (rc < 1 || rc > SN_MAX_CUTOFF) {
         why = "cutoff outside 1.." + std::to_string(SN_MAX_CUTOFF);
@@ -312,9 +315,11 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
         int balanced;
     };
     std::vector<Cand> all;
-    // SN_BLOCK="bx,by,bz" forces a block shape (for tuning); it must be valid
+    // a forced block shape (the replica's own, else SN_BLOCK="bx,by,bz"); it must be valid
     int force[3] = {0, 0, 0};
-    if (const char *env = getenv("SN_BLOCK")) {
+    if (force_shape && force_shape[0] > 0) {
+        for (int a = 0; a < 3; a++) force[a] = force_shape[a];
+    } else if (const char *env = getenv("SN_BLOCK")) {
         if (sscanf(env, "%d,%d,%d", &force[0], &force[1], &force[2]) != 3) force[0] = 0;
     }
     for (int bx : cands[0])
@@ -392,12 +397,29 @@ bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string
             t.smem_bytes = (int)sn_sweep::sn_carve(t.slots, t.tg, t.pc, NS, S, NF, mixed, 4).total;
             t.field_smem = (int)sn_sweep::sn_carve(t.slots, t.tg, 0, NS, S, NF, mixed, 8).total;
             if (t.smem_bytes > limit || t.field_smem > kSmemLimit || t.pc < pc_min) continue;
-            out = t;
-            return true;
+            bool seen = false;  // pass 1 meets pass 0's shapes again
+            for (const SnTile &o : outs) seen |= o.B[0] == t.B[0] && o.B[1] == t.B[1] && o.B[2] == t.B[2];
+            if (seen) continue;
+            outs.push_back(t);
+            if (outs.size() >= max_out) return true;
         }
     }
-    why = "no block shape fits in shared memory for this lattice and cutoff";
+    if (!outs.empty()) return true;
+    if (force[0])
+        why = "block shape " + std::to_string(force[0]) + "x" + std::to_string(force[1]) + "x" +
+              std::to_string(force[2]) + " does not tile this lattice (even block counts, blocks >= cutoff) or fit "
+                                         "in shared memory";
+    else
+        why = "no block shape fits in shared memory for this lattice and cutoff";
     return false;
+}
+
+bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string &why, const int *force = nullptr)
+{
+    std::vector<SnTile> v;
+    if (!plan_tiles(X, Y, Z, rc, mixed, v, 1, why, force)) return false;
+    out = v[0];
+    return true;
 }
 
 void fill_info(const SnTile &t, int rc, sn_schedule_info *o)
@@ -790,7 +812,7 @@ sn_status sn_check_flow(const sn_params *params, int n_replicas, const sn_replic
     std::vector<SnTile> tiles(n_replicas);
     std::string why;
     for (int r = 0; r < n_replicas; r++)
-        if (!plan_tile(replicas[r].X, replicas[r].Y, replicas[r].Z, P.cutoff, mixed, tiles[r], why))
+        if (!plan_tile(replicas[r].X, replicas[r].Y, replicas[r].Z, P.cutoff, mixed, tiles[r], why, replicas[r].block))
             return fail(nullptr, SN_ERR_SCHEDULE, "replica %d: %s", r, why.c_str());
     SnPlan pl;
     if (!build_plan(tiles, replicas, n_replicas, true, pl, why)) return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
@@ -849,6 +871,23 @@ sn_status sn_check_flow(const sn_params *params, int n_replicas, const sn_replic
         stats[1] = ndeps;
         stats[2] = maxd;
     }
+    return SN_OK;
+}
+
+sn_status sn_plan_candidates(int X, int Y, int Z, int cutoff, int mixed_lengths, sn_schedule_info *out,
+                             int max_out, int *n_out)
+{
+    if (!out || !n_out || max_out < 1 || X < 1 || Y < 1 || Z < 1)
+        return fail(nullptr, SN_ERR_ARG, "bad lattice size, null output or max_out < 1");
+    if (cutoff < 1 || cutoff > SN_MAX_CUTOFF)
+        return fail(nullptr, SN_ERR_UNSUPPORTED, "cutoff %d outside 1..%d", cutoff, SN_MAX_CUTOFF);
+    std::vector<SnTile> v;
+    std::string why;
+    *n_out = 0;
+    if (!plan_tiles(X, Y, Z, cutoff, mixed_lengths != 0, v, (size_t)max_out, why))
+        return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
+    for (size_t i = 0; i < v.size(); i++) fill_info(v[i], cutoff, &out[i]);
+    *n_out = (int)v.size();
     return SN_OK;
 }
 
@@ -958,7 +997,7 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     for (int r = 0; r < n_replicas; r++) {
         std::string why;
         const sn_replica_desc &d = replicas[r];
-        if (!plan_tile(d.X, d.Y, d.Z, P.cutoff, mixed, h->tiles[r], why))
+        if (!plan_tile(d.X, d.Y, d.Z, P.cutoff, mixed, h->tiles[r], why, d.block))
             return bail(fail(h, SN_ERR_SCHEDULE, "replica %d (%dx%dx%d): %s", r, d.X, d.Y, d.Z, why.c_str()));
         const long long N = (long long)d.X * d.Y * d.Z;
         float *mem = nullptr;

@@ -63,6 +63,7 @@ class Replica:
     T: float = 300.0
     efield: Sequence[float] | None = None
     seed: int = 0
+    block: Sequence[int] | None = None  # forced block shape (bx, by, bz); None: the planner's choice
 
     def to_c(self) -> _abi.ReplicaDesc:
         d = _abi.ReplicaDesc()
@@ -72,6 +73,9 @@ class Replica:
             for k in range(3):
                 d.efield[k] = float(self.efield[k])
         d.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        if self.block is not None:
+            for k in range(3):
+                d.block[k] = int(self.block[k])
         return d
 
     @property
@@ -83,6 +87,14 @@ def plan_schedule(X: int, Y: int, Z: int, cutoff: int, mixed: bool = False) -> d
     info = _abi.ScheduleInfo()
     check(lib().sn_plan_schedule(X, Y, Z, cutoff, int(mixed), ctypes.byref(info)))
     return info.as_dict()
+
+
+def plan_candidates(X: int, Y: int, Z: int, cutoff: int, mixed: bool = False, max_out: int = 8) -> list:
+    """Feasible schedules in the planner's preference order (host-only)."""
+    arr = (_abi.ScheduleInfo * max_out)()
+    n = ctypes.c_int(0)
+    check(lib().sn_plan_candidates(X, Y, Z, cutoff, int(mixed), arr, max_out, ctypes.byref(n)))
+    return [arr[i].as_dict() for i in range(n.value)]
 
 
 def check_schedule(X: int, Y: int, Z: int, cutoff: int, sched: dict) -> bool:

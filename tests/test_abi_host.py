@@ -91,3 +91,26 @@ def test_dataflow_schedule_is_complete_and_acyclic(native_lib):
             [sn.plan_schedule(r.X, r.Y, r.Z, params.cutoff, mixed=len({d for d in params.dipoles if d > 0}) > 1)[k]
              for k in ("bx", "by", "bz")])) for r in reps), name
         assert 0 < st["max_dependencies"] <= 26, name  # the 26 neighbours of a last-colour block
+
+
+def test_plan_candidates_and_forced_shapes(native_lib):
+    """The candidate list starts with the planner's choice, every candidate is a
+    conflict-free schedule, and a replica can be given any of them -- but not a shape
+    that does not tile its lattice."""
+    sn = native_lib
+    for (X, Y, Z), rc, mixed in (((256, 256, 256), 3, False), ((96, 96, 96), 5, False), ((64, 48, 32), 3, True),
+                                 ((2048, 2048, 1), 5, False)):
+        cands = sn.plan_candidates(X, Y, Z, rc, mixed, max_out=6)
+        assert 1 <= len(cands) <= 6
+        assert cands[0] == sn.plan_schedule(X, Y, Z, rc, mixed)
+        shapes = [(c["bx"], c["by"], c["bz"]) for c in cands]
+        assert len(set(shapes)) == len(shapes)
+        params = sn.ModelParams(cutoff=rc, dipoles=(1.0, 0.5) if mixed else (1.0,),
+                                prevalence=(0.5, 0.5) if mixed else (1.0,))
+        for c, shape in zip(cands, shapes):
+            if X * Y * Z <= 100_000:  # brute-force check, small lattices only
+                assert sn.check_schedule(X, Y, Z, rc, c)
+            st = sn.check_flow(params, [sn.Replica(X, Y, Z, block=shape)])
+            assert st["blocks"] == (X // shape[0]) * (Y // shape[1]) * (Z // shape[2])
+    with pytest.raises(sn.SnError, match="does not tile"):
+        sn.check_flow(sn.ModelParams(cutoff=3), [sn.Replica(64, 64, 64, block=(5, 8, 8))])
