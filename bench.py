@@ -11,8 +11,9 @@ Workload (one "step" = one Metropolis sweep of the lattice):
 Metric: attempted Metropolis updates of occupied sites per second
 ("dipole site-updates/s"), whole job.  `value` is device-resident (lattice in
 HBM, CUDA events on the library's stream around K sweeps); `e2e` goes through
-the C ABI with pinned HOST buffers every step: upload the lattice, one sweep,
-download the lattice, read the observables -- the drop-in for one
+the C ABI with pinned HOST buffers every step: upload the lattice, one sweep
+that writes each block's final sites into the host buffer as the block ends
+(sn_gpu_sweep_download), read the observables -- the drop-in for one
 MC_moves(X*Y*Z) call of the reference on a host lattice.
 
 `--impl reference` times the reference's CPU algorithm (random-sequential
@@ -358,22 +359,21 @@ def run_ours(args, ws, rank, local):
         hx = torch.empty(3 * N, dtype=torch.float32, pin_memory=True)
         hl = torch.empty(N, dtype=torch.float32, pin_memory=True)
         sim.download_ptr(0, hx.data_ptr(), hl.data_ptr())
-        for _ in range(2):
+        for _ in range(3):
             sim.upload_ptr(0, hx.data_ptr(), hl.data_ptr())
-            sim.sweep(1)
-            sim.download_ptr(0, hx.data_ptr(), None)
+            sim.sweep_download(1, [hx.data_ptr()])
             sim.observables()
         dist_barrier(ws)
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             sim.upload_ptr(0, hx.data_ptr(), hl.data_ptr())
-            sim.sweep(1)
-            sim.download_ptr(0, hx.data_ptr(), None)
+            sim.sweep_download(1, [hx.data_ptr()])
             sim.observables()
         dt = dist_max(ws, time.perf_counter() - t0)
         e2e = {"value": dist_sum(ws, float(occ) * args.e2e_steps) / dt, "unit": "site-updates/s",
                "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 12 * N + 40,
-               "step": "upload lattice (xyz+len) from pinned host memory, 1 sweep, download xyz, observables"}
+               "step": "upload lattice (xyz+len) from pinned host memory, 1 sweep writing its final xyz into the "
+                       "pinned host buffer (sn_gpu_sweep_download), observables"}
     batched = None
     if not args.no_batched and ws == 1:
         batched = run_batched(sn, torch)

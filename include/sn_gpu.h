@@ -148,6 +148,17 @@ sn_status sn_gpu_download_lattice(sn_handle *h, int replica, float *xyz, float *
  * (src/starrynight-montecarlo-core.c:143-191) and the ACCEPT/REJECT counters. */
 sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *reject);
 
+/* sn_gpu_sweep, then the lattice of every replica r with xyz[r] != NULL
+ * written to xyz[r] (3 floats per site, as sn_gpu_download_lattice with a
+ * NULL len); xyz has one entry per replica.  A buffer in pinned or
+ * registered host memory (or device memory) is written by the last sweep
+ * itself, each block's sites as soon as that block is final, so the
+ * transfer overlaps the sweep; any other buffer is filled by the staged
+ * download afterwards.  The same lattice either way.  Replaces MC_moves on
+ * the host lattice followed by the read of lattice[x][y][z] by the output
+ * routines (src/starrynight-main.c:222-227, :248). */
+sn_status sn_gpu_sweep_download(sn_handle *h, int n_sweeps, float *const *xyz, uint64_t *accept, uint64_t *reject);
+
 /* Total sweeps done so far (the Philox sweep counter). */
 sn_status sn_gpu_sweep_count(const sn_handle *h, uint64_t *sweeps);
 

@@ -86,6 +86,7 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_upload_lattice": ([h, _i, _vp, _vp], _i),
             "sn_gpu_download_lattice": ([h, _i, _vp, _vp], _i),
             "sn_gpu_sweep": ([h, _i, _P(ctypes.c_uint64), _P(ctypes.c_uint64)], _i),
+            "sn_gpu_sweep_download": ([h, _i, _P(ctypes.c_void_p), _P(ctypes.c_uint64), _P(ctypes.c_uint64)], _i),
             "sn_gpu_sweep_count": ([h, _P(ctypes.c_uint64)], _i),
             "sn_gpu_set_sweep_count": ([h, ctypes.c_uint64], _i),
             "sn_gpu_energy": ([h, _i, _i, _P(ctypes.c_double), _vp], _i),

@@ -471,7 +471,7 @@ struct sn_handle {
     int rc = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // host transfers overlapped with work on `stream`
-    static constexpr int kSlabs = 8;
+    static constexpr int kSlabs = SN_UPLOAD_SLABS;
     cudaEvent_t slab_ev[kSlabs] = {};
     std::vector<sn_replica_desc> desc;
     std::vector<SnTile> tiles;
@@ -1219,18 +1219,69 @@ sn_status sn_gpu_download_lattice(sn_handle *h, int replica, float *xyz, float *
     return flow_status(h);
 }
 
-sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *reject)
+namespace {
+
+// Address under which kernels may write a caller's buffer of n floats:
+// pinned or registered host memory (mapped) or this device's memory, checked
+// at both ends; nullptr for anything else (pageable memory goes through the
+// staged download).
+float *device_view(float *p, size_t n)
 {
-    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
-    if (n_sweeps < 0) return fail(h, SN_ERR_ARG, "negative sweep count");
+    int dev = -1;
+    if (!p || n == 0 || cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    cudaPointerAttributes a0, a1;
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess || cudaPointerGetAttributes(&a1, p + (n - 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    const bool host = a0.type == cudaMemoryTypeHost && a1.type == cudaMemoryTypeHost;
+    const bool devm = a0.type == cudaMemoryTypeDevice && a1.type == cudaMemoryTypeDevice && a0.device == dev &&
+                      a1.device == dev;
+    if (!(host || devm) || !a0.devicePointer || !a1.devicePointer) return nullptr;
+    float *d0 = static_cast<float *>(a0.devicePointer), *d1 = static_cast<float *>(a1.devicePointer);
+    return d1 == d0 + (n - 1) ? d0 : nullptr;
+}
+
+// n sweeps; outs (nrep entries, nullable) are device views that the last
+// sweep writes its final sites to.  Every pointer set here is cleared again
+// before returning, also on failure.
+sn_status run_sweeps(sn_handle *h, int n_sweeps, float *const *outs, uint64_t *accept, uint64_t *reject)
+{
     std::vector<SnState> before;
     if (accept || reject) {
         before.resize(h->nrep);
         SN_CK(h, cudaMemcpyAsync(before.data(), h->d_state, h->nrep * sizeof(SnState), cudaMemcpyDeviceToHost,
                                  h->stream));
     }
+    bool armed = false;
+    auto disarm = [&]() {
+        for (int r = 0; outs && armed && r < h->nrep; r++)
+            if (outs[r]) sn_launch_set_out(h->d_reps, r, nullptr, h->stream);
+        armed = false;
+    };
     for (int i = 0; i < n_sweeps; i++) {
-        SN_CK(h, cudaGraphLaunch(h->graph, h->stream));
+        if (outs && i == n_sweeps - 1) {
+            armed = true;
+            for (int r = 0; r < h->nrep; r++) {
+                if (!outs[r]) continue;
+                const cudaError_t e = sn_launch_set_out(h->d_reps, r, outs[r], h->stream);
+                if (e != cudaSuccess) {
+                    disarm();
+                    return fail(h, SN_ERR_CUDA, "%s", cudaGetErrorString(e));
+                }
+                h->launches++;
+            }
+        }
+        const cudaError_t e = cudaGraphLaunch(h->graph, h->stream);
+        if (e != cudaSuccess) {
+            disarm();
+            return fail(h, SN_ERR_CUDA, "%s", cudaGetErrorString(e));
+        }
+        if (armed) {
+            for (int r = 0; r < h->nrep; r++)
+                if (outs[r]) h->launches++;
+            disarm();
+        }
         h->launches += h->graph_nodes;
         h->sweeps++;
         if (h->recompute_every > 0 && h->sweeps % (uint64_t)h->recompute_every == 0) {
@@ -1256,6 +1307,36 @@ sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *r
         if (s) return s;
     }
     SN_CK(h, cudaGetLastError());
+    return SN_OK;
+}
+
+}  // namespace
+
+sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *reject)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    if (n_sweeps < 0) return fail(h, SN_ERR_ARG, "negative sweep count");
+    return run_sweeps(h, n_sweeps, nullptr, accept, reject);
+}
+
+sn_status sn_gpu_sweep_download(sn_handle *h, int n_sweeps, float *const *xyz, uint64_t *accept, uint64_t *reject)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    if (n_sweeps < 0) return fail(h, SN_ERR_ARG, "negative sweep count");
+    if (!xyz) return fail(h, SN_ERR_ARG, "null buffer table");
+    std::vector<float *> outs(h->nrep, nullptr);
+    bool any = false;
+    for (int r = 0; r < h->nrep; r++) {
+        if (!xyz[r]) continue;
+        outs[r] = device_view(xyz[r], 3 * (size_t)h->reps[r].n_sites);
+        any |= outs[r] != nullptr;
+    }
+    sn_status s = run_sweeps(h, n_sweeps, (any && n_sweeps > 0) ? outs.data() : nullptr, accept, reject);
+    if (s) return s;
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    if ((s = flow_status(h))) return s;
+    for (int r = 0; r < h->nrep; r++)  // buffers the kernels cannot write (or no sweep ran)
+        if (xyz[r] && (!outs[r] || n_sweeps == 0) && (s = sn_gpu_download_lattice(h, r, xyz[r], nullptr))) return s;
     return SN_OK;
 }
 

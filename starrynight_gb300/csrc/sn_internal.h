@@ -25,6 +25,10 @@
 #define SN_ACC_SETS 2
 #endif
 #define SN_SWEEP_MAX_THREADS (SN_TWO_PER_SM_THREADS > 256 ? SN_TWO_PER_SM_THREADS : SN_MAX_THREADS)
+// x slabs of a host upload (each converted and fed to the energy pass as it lands).
+#ifndef SN_UPLOAD_SLABS
+#define SN_UPLOAD_SLABS 16
+#endif
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log
 
@@ -63,6 +67,10 @@ struct SnReplicaDev {
     float E[3];        // applied field
     float length;      // uniform dipole length (uniform mode)
     uint32_t seed_lo, seed_hi;
+    // Set for one sweep by sn_gpu_sweep_download: a buffer the GPU can write
+    // (mapped pinned host memory or device memory) that receives every
+    // block's final sites (x, y, z per site, site order) as the block ends.
+    float *out_xyz;
 };
 
 // Per-replica sweep accumulators (zeroed at the end of every sweep).

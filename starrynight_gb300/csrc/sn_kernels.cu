@@ -83,6 +83,11 @@ __global__ void download_convert_kernel(const float *__restrict__ px, const floa
     }
 }
 
+__global__ void set_out_kernel(SnReplicaDev *reps, int r, float *out)
+{
+    if (threadIdx.x == 0) reps[r].out_xyz = out;
+}
+
 // End of one sweep: fold the per-sweep accumulators into the running FP64
 // totals, log E/site and |P|/site, advance the sweep counter and, when due,
 // run one round of replica exchange between adjacent temperatures.
@@ -249,6 +254,12 @@ cudaError_t sn_launch_download_convert(const float *px, const float *py, const f
                                        float *stage_xyz, float *stage_len, long long n, cudaStream_t st)
 {
     download_convert_kernel<<<grid_for(n, 256), 256, 0, st>>>(px, py, pz, len, stage_xyz, stage_len, n);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_set_out(SnReplicaDev *reps, int r, float *out, cudaStream_t st)
+{
+    set_out_kernel<<<1, 32, 0, st>>>(reps, r, out);
     return cudaGetLastError();
 }
 

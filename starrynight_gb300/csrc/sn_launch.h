@@ -79,6 +79,8 @@ cudaError_t sn_launch_upload_convert(const float *stage_xyz, const float *stage_
                                      int *flags, cudaStream_t st);
 cudaError_t sn_launch_download_convert(const float *px, const float *py, const float *pz, const float *len,
                                        float *stage_xyz, float *stage_len, long long n, cudaStream_t st);
+// reps[r].out_xyz = out (nullptr: the sweep writes no copy), in stream order.
+cudaError_t sn_launch_set_out(SnReplicaDev *reps, int r, float *out, cudaStream_t st);
 cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnReplicaDev *reps, int nrep,
                                 uint32_t *sweep, SnExchange *ex, int *order, uint32_t *queues, cudaStream_t st);
 cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const SnReplicaDev *reps, int rep,

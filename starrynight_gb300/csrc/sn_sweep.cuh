@@ -474,6 +474,20 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
         __syncthreads();
     }
 
+    // ---- the block's final sites to the caller's buffer -------------------------
+    // No other block writes these sites during the sweep, so the tile's
+    // interior is final now.  A row of the block (fixed x, y) is 3*Bz floats
+    // contiguous both in the tile (z stored plainly) and in the buffer.
+    if (float *out = R.out_xyz) {
+        const int w3 = 3 * Bz;
+        for (int row = warp; row < Bx * By; row += nthreads >> 5) {
+            const int lx = row / By, ly = row - (row / By) * By;
+            const int s0 = sn_pi<S>(start, lx + H) * Sx + sn_pi<S>(start + SN_MAX_S, ly + H) * Sy + HZ;
+            const long long o0 = 3ll * ((((long long)(w.x0 + lx)) * Y + (w.y0 + ly)) * Z + (TWO_D ? 0 : w.z0));
+            for (int e = lane; e < w3; e += 32) out[o0 + e] = tile[3 * s0 + e];
+        }
+    }
+
     // ---- block reduction of the move statistics ---------------------------------
     double v[6] = {sdE.value(), sPx.value(), sPy.value(), sPz.value(), (double)sacc, (double)satt};
 #pragma unroll

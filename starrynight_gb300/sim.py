@@ -210,6 +210,30 @@ class Simulation:
         self._ck(lib().sn_gpu_sweep(self._h, int(n), None, None))
         return None
 
+    def sweep_download(self, n: int, outs, counts: bool = False):
+        """n sweeps, then each replica's lattice into outs[r] (numpy (N, 3) float32,
+        a raw pointer, or None to skip).  Pinned buffers are written by the last
+        sweep itself; others by the staged download."""
+        if len(outs) != len(self.replicas):
+            raise ValueError("one output per replica")
+        tab = (ctypes.c_void_p * len(outs))()
+        keep = []
+        for r, o in enumerate(outs):
+            if o is None:
+                continue
+            if isinstance(o, int):
+                tab[r] = o
+            else:
+                if not (isinstance(o, np.ndarray) and o.dtype == np.float32 and o.flags.c_contiguous
+                        and o.size == 3 * self.n_sites(r)):
+                    raise ValueError("replica %d: need a C-contiguous float32 array of %d values" % (r, 3 * self.n_sites(r)))
+                keep.append(o)
+                tab[r] = o.ctypes.data
+        a, j = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        self._ck(lib().sn_gpu_sweep_download(self._h, int(n), tab, ctypes.byref(a) if counts else None,
+                                             ctypes.byref(j) if counts else None))
+        return (a.value, j.value) if counts else None
+
     def sweep_count(self) -> int:
         v = ctypes.c_uint64(0)
         self._ck(lib().sn_gpu_sweep_count(self._h, ctypes.byref(v)))
