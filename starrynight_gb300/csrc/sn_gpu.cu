@@ -473,6 +473,11 @@ struct sn_handle {
     cudaStream_t copy_stream = nullptr;  // host transfers overlapped with work on `stream`
     static constexpr int kSlabs = SN_UPLOAD_SLABS;
     cudaEvent_t slab_ev[kSlabs] = {};
+    // upload: the energy pass runs in chunks alternating between two streams,
+    // so one chunk's last wave overlaps the next chunk's first
+    cudaStream_t field_stream[2] = {};
+    cudaEvent_t conv_ev[kSlabs] = {};
+    cudaEvent_t fdone_ev[2] = {};
     std::vector<sn_replica_desc> desc;
     std::vector<SnTile> tiles;
     std::vector<SnReplicaDev> reps;
@@ -591,14 +596,14 @@ sn_status launch_field(sn_handle *h, int r, bool fp64, const SnFieldArgsHost &a)
 
 // Field pass over the blocks bx in [b0, b1) of replica r (the replica's block
 // list is x-major, so they are contiguous).
-sn_status launch_field_x(sn_handle *h, int r, const SnFieldArgsHost &base, int b0, int b1)
+sn_status launch_field_x(sn_handle *h, int r, const SnFieldArgsHost &base, int b0, int b1, cudaStream_t st)
 {
     if (b1 <= b0) return SN_OK;
     const SnTile &t = h->tiles[r];
     SnFieldArgsHost a = base;
     a.work = base.work + (size_t)b0 * t.nb[1] * t.nb[2];
     SN_CK(h, k_field[h->rc](false, h->desc[r].Z == 1, h->mixed, &a, (b1 - b0) * t.nb[1] * t.nb[2], t.threads,
-                            t.field_smem, h->stream));
+                            t.field_smem, st));
     h->launches++;
     return SN_OK;
 }
@@ -741,6 +746,12 @@ void destroy_all(sn_handle *h)
         if (p) cudaFree(p);
     for (auto &e : h->slab_ev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : h->conv_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : h->fdone_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &f : h->field_stream)
+        if (f) cudaStreamDestroy(f);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -988,9 +999,15 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         return s;
     };
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+        cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->field_stream[0], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->field_stream[1], cudaStreamNonBlocking) != cudaSuccess)
         return bail(fail(h, SN_ERR_CUDA, "cudaStreamCreate failed"));
-    for (auto &e : h->slab_ev)
+    for (auto *evs : {&h->slab_ev[0], &h->conv_ev[0]})
+        for (int k = 0; k < sn_handle::kSlabs; k++)
+            if (cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming) != cudaSuccess)
+                return bail(fail(h, SN_ERR_CUDA, "cudaEventCreate failed"));
+    for (auto &e : h->fdone_ev)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(h, SN_ERR_CUDA, "cudaEventCreate failed"));
 
@@ -1155,8 +1172,10 @@ sn_status sn_gpu_upload_lattice(sn_handle *h, int replica, const float *xyz, con
     // The copy runs in x slabs (whole block rows) on the copy stream; each slab
     // is converted as soon as it lands, and the energy pass of the running
     // total starts on every block whose tile (block + halo) has fully arrived,
-    // so the transfer and the recompute overlap.  Blocks whose halo wraps past
-    // x = 0 or X go last.
+    // so the transfer and the recompute overlap.  Those energy chunks
+    // alternate between two streams (a chunk reads only converted slabs, and
+    // the conversions write slabs no running chunk reads).  Blocks whose halo
+    // wraps past x = 0 or X go last.
     const int nb = t.nb[0], Bx = t.B[0], H = h->rc;
     const int Q = std::max(1, std::min(sn_handle::kSlabs, nb));
     const size_t row = (size_t)R.Y * R.Z;
@@ -1181,13 +1200,20 @@ sn_status sn_gpu_upload_lattice(sn_handle *h, int replica, const float *xyz, con
                                           R.py + a0, R.pz + a0, R.len + a0, (long long)cnt, h->length,
                                           h->mixed ? 1 : 0, h->params.dipoles[0], h->d_flags, h->stream));
         h->launches++;
+        SN_CK(h, cudaEventRecord(h->conv_ev[q], h->stream));
+        cudaStream_t fs = h->field_stream[SN_UPLOAD_FIELD_STREAMS > 1 ? (q & 1) : 0];
+        SN_CK(h, cudaStreamWaitEvent(fs, h->conv_ev[q], 0));
         // blocks whose tile x range [b*Bx - H, (b+1)*Bx + H) lies in [0, x1)
         int last = (x1 - H) / Bx - 1;
         if (q == Q - 1) last = nb - 1;
-        if ((s = launch_field_x(h, replica, fa, next_b, last + 1))) return s;
+        if ((s = launch_field_x(h, replica, fa, next_b, last + 1, fs))) return s;
         next_b = std::max(next_b, last + 1);
     }
-    if ((s = launch_field_x(h, replica, fa, 0, 1))) return s;
+    for (int k = 0; k < 2; k++) {
+        SN_CK(h, cudaEventRecord(h->fdone_ev[k], h->field_stream[k]));
+        SN_CK(h, cudaStreamWaitEvent(h->stream, h->fdone_ev[k], 0));
+    }
+    if ((s = launch_field_x(h, replica, fa, 0, 1, h->stream))) return s;
     SN_CK(h, sn_launch_recompute_finish(red, h->d_state, h->d_reps, replica, h->params.cage_strain, h->d_drift, 0,
                                         h->stream));
     h->launches++;

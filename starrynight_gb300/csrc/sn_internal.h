@@ -25,9 +25,14 @@
 #define SN_ACC_SETS 2
 #endif
 #define SN_SWEEP_MAX_THREADS (SN_TWO_PER_SM_THREADS > 256 ? SN_TWO_PER_SM_THREADS : SN_MAX_THREADS)
-// x slabs of a host upload (each converted and fed to the energy pass as it lands).
+// x slabs of a host upload (each converted and fed to the energy pass as it
+// lands); 8 measured faster than 16 at 256^3 (2.00 vs 2.24 ms).
 #ifndef SN_UPLOAD_SLABS
-#define SN_UPLOAD_SLABS 16
+#define SN_UPLOAD_SLABS 8
+#endif
+// streams the upload's energy-pass chunks alternate between (1 or 2)
+#ifndef SN_UPLOAD_FIELD_STREAMS
+#define SN_UPLOAD_FIELD_STREAMS 2
 #endif
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log
