@@ -159,6 +159,14 @@ sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *r
  * routines (src/starrynight-main.c:222-227, :248). */
 sn_status sn_gpu_sweep_download(sn_handle *h, int n_sweeps, float *const *xyz, uint64_t *accept, uint64_t *reject);
 
+/* Page-locked host memory for the lattice buffers of the calls above, for C
+ * hosts that do not include the CUDA headers: uploads and downloads from it
+ * run at the full host-link rate and sn_gpu_sweep_download writes it from
+ * the sweep itself.  NULL on failure; free with sn_gpu_host_free.  (The
+ * reference allocates its lattice with malloc, src/starrynight-main.c:155-161.) */
+void *sn_gpu_host_alloc(size_t bytes);
+void sn_gpu_host_free(void *p);
+
 /* Total sweeps done so far (the Philox sweep counter). */
 sn_status sn_gpu_sweep_count(const sn_handle *h, uint64_t *sweeps);
 

@@ -82,6 +82,8 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_destroy": ([h], _i),
             "sn_gpu_status_string": ([_i], ctypes.c_char_p),
             "sn_gpu_last_error": ([h], ctypes.c_char_p),
+            "sn_gpu_host_alloc": ([ctypes.c_size_t], _vp),
+            "sn_gpu_host_free": ([_vp], None),
             "sn_gpu_init_lattice": ([h, _i, _i, ctypes.c_uint64], _i),
             "sn_gpu_upload_lattice": ([h, _i, _vp, _vp], _i),
             "sn_gpu_download_lattice": ([h, _i, _vp, _vp], _i),
@@ -140,4 +142,4 @@ def exported_names() -> list:
     import re
     hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "sn_gpu.h")
     src = open(hdr).read()
-    return sorted(set(re.findall(r"^\s*(?:sn_status|const char \*|int|void \*)\s*\*?\s*(sn_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:sn_status|const char \*|int|void \*|void)\s*\*?\s*(sn_\w+)\s*\(", src, re.M)))

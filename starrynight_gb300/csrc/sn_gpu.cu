@@ -1345,6 +1345,21 @@ sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *r
     return run_sweeps(h, n_sweeps, nullptr, accept, reject);
 }
 
+void *sn_gpu_host_alloc(size_t bytes)
+{
+    void *p = nullptr;
+    if (bytes == 0 || cudaMallocHost(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void sn_gpu_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
+}
+
 sn_status sn_gpu_sweep_download(sn_handle *h, int n_sweeps, float *const *xyz, uint64_t *accept, uint64_t *reject)
 {
     if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");

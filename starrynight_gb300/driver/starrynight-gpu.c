@@ -209,6 +209,7 @@ typedef struct {
     int have_lattice, have_pot;
     float dmax;
     FILE *log;
+    int pinned; /* xyz and len from sn_gpu_host_alloc */
 } ana_t;
 
 static int ana_fail(ana_t *a, const char *what, sn_status s)
@@ -473,8 +474,16 @@ int main(int argc, char **argv)
         a.c = &c;
         a.N = N;
         a.dmax = 55.0f;
-        a.xyz = (float *)malloc(3 * N * sizeof(float));
-        a.len = (float *)malloc(N * sizeof(float));
+        /* page-locked when the device allows: lattice downloads at the host-link rate */
+        a.xyz = (float *)sn_gpu_host_alloc(3 * N * sizeof(float));
+        a.len = (float *)sn_gpu_host_alloc(N * sizeof(float));
+        a.pinned = a.xyz && a.len;
+        if (!a.pinned) {
+            sn_gpu_host_free(a.xyz);
+            sn_gpu_host_free(a.len);
+            a.xyz = (float *)malloc(3 * N * sizeof(float));
+            a.len = (float *)malloc(N * sizeof(float));
+        }
         if (!a.xyz || !a.len) {
             fprintf(stderr, "out of host memory\n");
             sn_gpu_destroy(h);
@@ -557,8 +566,13 @@ int main(int argc, char **argv)
         fprintf(stderr, "Monte Carlo moves - ACCEPT: %llu REJECT: %llu ratio: %f\n", ACCEPT, REJECT,
                 (float)ACCEPT / (float)(REJECT + ACCEPT));
         fclose(a.log);
-        free(a.xyz);
-        free(a.len);
+        if (a.pinned) {
+            sn_gpu_host_free(a.xyz);
+            sn_gpu_host_free(a.len);
+        } else {
+            free(a.xyz);
+            free(a.len);
+        }
         free(a.pot);
         free(a.map);
         sn_gpu_destroy(h);

@@ -114,3 +114,11 @@ def test_plan_candidates_and_forced_shapes(native_lib):
             assert st["blocks"] == (X // shape[0]) * (Y // shape[1]) * (Z // shape[2])
     with pytest.raises(sn.SnError, match="does not tile"):
         sn.check_flow(sn.ModelParams(cutoff=3), [sn.Replica(64, 64, 64, block=(5, 8, 8))])
+
+
+def test_host_alloc_without_a_device_is_null_not_a_crash(native_lib):
+    L = _abi.lib()
+    assert not L.sn_gpu_host_alloc(0)
+    p = L.sn_gpu_host_alloc(64)  # NULL here (no GPU); a pointer where one exists
+    L.sn_gpu_host_free(p)
+    L.sn_gpu_host_free(None)

@@ -62,3 +62,24 @@ def test_sweep_download_headline_lattice(native_lib):
         acc, rej = sim.sweep_download(2, [buf.data_ptr()], counts=True)
         assert 0 < acc < acc + rej
         assert np.array_equal(buf.numpy().reshape(-1, 3), sim.download(0)[0])
+
+
+def test_abi_pinned_buffer(native_lib):
+    """A buffer from sn_gpu_host_alloc (page-locked, for C hosts without CUDA
+    headers) takes the in-sweep write-out."""
+    import ctypes
+    from starrynight_gb300._abi import lib
+    sn = native_lib
+    params = sn.ModelParams(cutoff=2, efield=(0.05, 0.0, 0.0), seed=9)
+    rep = sn.Replica(24, 24, 24, T=200.0, seed=9)
+    n = 3 * rep.n_sites
+    p = lib().sn_gpu_host_alloc(4 * n)
+    assert p
+    try:
+        with sn.Simulation(params, [rep]) as sim:
+            sim.init_lattice(0)
+            sim.sweep_download(2, [p])
+            got = np.ctypeslib.as_array((ctypes.c_float * n).from_address(p)).reshape(-1, 3).copy()
+            assert np.array_equal(got, sim.download(0)[0])
+    finally:
+        lib().sn_gpu_host_free(p)
