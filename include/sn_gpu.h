@@ -305,6 +305,15 @@ sn_status sn_plan_schedule(int X, int Y, int Z, int cutoff, int mixed_lengths, s
  * sn_replica_desc.block. */
 sn_status sn_plan_candidates(int X, int Y, int Z, int cutoff, int mixed_lengths, sn_schedule_info *out,
                              int max_out, int *n_out);
+/* The empirical autotuner: times the first max_candidates of
+ * sn_plan_candidates for this replica's lattice size (one temporary handle
+ * each, a random lattice at the replica's temperature and field, 2 warm-up
+ * sweeps, then `sweeps` sweeps timed with CUDA events) and writes the
+ * fastest shape to block[3] and its time to *ms_per_sweep (nullable).  Put
+ * block into sn_replica_desc.block; every shape gives an exact sweep, the
+ * choice only changes speed and the order of the moves. */
+sn_status sn_gpu_autotune(const sn_params *params, const sn_replica_desc *replica, int max_candidates, int sweeps,
+                          int block[3], double *ms_per_sweep);
 /* Host-only: 1 if no two sites updated together interact under periodic
  * boundaries (same block colour and site colour within the cutoff). */
 int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *sched);

@@ -107,6 +107,7 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_schedule": ([h, _i, _P(ScheduleInfo)], _i),
             "sn_plan_schedule": ([_i, _i, _i, _i, _i, _P(ScheduleInfo)], _i),
             "sn_plan_candidates": ([_i, _i, _i, _i, _i, _P(ScheduleInfo), _i, _P(_i)], _i),
+            "sn_gpu_autotune": ([_P(Params), _P(ReplicaDesc), _i, _i, _P(_i), _P(ctypes.c_double)], _i),
             "sn_check_schedule": ([_i, _i, _i, _i, _P(ScheduleInfo)], _i),
             "sn_check_flow": ([_P(Params), _i, _P(ReplicaDesc), _vp], _i),
             "sn_gpu_launch_count": ([h, _P(ctypes.c_uint64)], _i),

@@ -13,9 +13,11 @@ differ); the tuned shape is a per-lattice-size choice a run keeps fixed.
 """
 from __future__ import annotations
 
+import ctypes
 import dataclasses
 from typing import Sequence
 
+from ._abi import check, lib
 from .sim import ModelParams, Replica, Simulation, plan_candidates
 
 
@@ -51,3 +53,14 @@ def tune_table(params: ModelParams, replicas: Sequence[Replica], **kw) -> list:
             chosen[key] = tune(params, r, **kw)[0]
         out.append(dataclasses.replace(r, block=chosen[key]))
     return out
+
+
+def tune_native(params: ModelParams, replica: Replica, max_candidates: int = 6, sweeps: int = 5) -> tuple:
+    """The same choice made inside the C ABI (``sn_gpu_autotune``, what a C host
+    calls): ((bx, by, bz), ms per sweep of that shape)."""
+    blk = (ctypes.c_int * 3)()
+    ms = ctypes.c_double(0.0)
+    cp, d = params.to_c(), replica.to_c()
+    check(lib().sn_gpu_autotune(ctypes.byref(cp), ctypes.byref(d), int(max_candidates), int(sweeps), blk,
+                                ctypes.byref(ms)))
+    return (blk[0], blk[1], blk[2]), ms.value

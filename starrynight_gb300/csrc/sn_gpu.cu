@@ -902,6 +902,56 @@ sn_status sn_plan_candidates(int X, int Y, int Z, int cutoff, int mixed_lengths,
     return SN_OK;
 }
 
+sn_status sn_gpu_autotune(const sn_params *params, const sn_replica_desc *replica, int max_candidates, int sweeps,
+                          int block[3], double *ms_per_sweep)
+{
+    if (!params || !replica || !block || max_candidates < 1 || sweeps < 1)
+        return fail(nullptr, SN_ERR_ARG, "null argument, max_candidates < 1 or sweeps < 1");
+    bool mixed = false;
+    float L = 0.0f;
+    for (int i = 0; i < params->n_species && i < SN_MAX_SPECIES; i++) {
+        const float d = params->dipoles[i];
+        if (d > 0.0f) {
+            if (L == 0.0f) L = d;
+            else if (d != L) mixed = true;
+        }
+    }
+    std::vector<sn_schedule_info> cands((size_t)max_candidates);
+    int n = 0;
+    sn_status s = sn_plan_candidates(replica->X, replica->Y, replica->Z, params->cutoff, mixed ? 1 : 0, cands.data(),
+                                     max_candidates, &n);
+    if (s) return s;
+    double best = 0.0;
+    int best_shape[3] = {0, 0, 0};
+    for (int i = 0; i < n; i++) {
+        sn_replica_desc d = *replica;
+        d.block[0] = cands[i].bx;
+        d.block[1] = cands[i].by;
+        d.block[2] = cands[i].bz;
+        sn_handle *h = nullptr;
+        if ((s = sn_gpu_init(params, 1, &d, &h))) return s;
+        double launch_ms = 0.0, ms = 0.0;
+        int nl = 0;
+        s = sn_gpu_init_lattice(h, 0, SN_LATTICE_RANDOM, 0);
+        if (!s) s = sn_gpu_sweep(h, 2, nullptr, nullptr);  // warm-up
+        if (!s) s = sn_gpu_phase_times(h, sweeps, &launch_ms, &ms, &nl);
+        if (!s) s = flow_status(h);
+        if (s) {
+            const std::string msg = h->err;
+            sn_gpu_destroy(h);
+            return fail(nullptr, s, "block %dx%dx%d: %s", d.block[0], d.block[1], d.block[2], msg.c_str());
+        }
+        sn_gpu_destroy(h);
+        if (i == 0 || ms < best) {
+            best = ms;
+            for (int k = 0; k < 3; k++) best_shape[k] = d.block[k];
+        }
+    }
+    for (int k = 0; k < 3; k++) block[k] = best_shape[k];
+    if (ms_per_sweep) *ms_per_sweep = best;
+    return SN_OK;
+}
+
 int sn_check_schedule(int X, int Y, int Z, int cutoff, const sn_schedule_info *sc)
 {
     if (!sc || X < 1 || Y < 1 || Z < 1 || cutoff < 1) return 0;

@@ -29,7 +29,9 @@
  * src/starrynight-main.c:172), ResumeFrom (a checkpoint file that replaces
  * InitialLattice and restores the sweep counter), CheckpointFile and
  * CheckpointEvery (write a checkpoint every that many production
- * megasteps, and at the end).  Options: --config FILE, --seed N,
+ * megasteps, and at the end), AutoTune (time that many of the planner's
+ * block shapes with sn_gpu_autotune and run with the fastest; 0 = the
+ * planner's choice).  Options: --config FILE, --seed N,
  * --print-config (parse, print, exit without touching the GPU).
  */
 #include <math.h>
@@ -61,6 +63,7 @@ typedef struct {
     unsigned long long seed;
     char resume[256], checkpoint[256];
     int checkpoint_every;
+    int autotune;
 } cfg_t;
 
 /* Defaults of src/starrynight-config.c:12-93 (the reference leaves T and
@@ -145,6 +148,7 @@ static int cfg_load(const char *path, cfg_t *c)
     if (config_lookup_string(&cf, "ResumeFrom", &str)) snprintf(c->resume, sizeof(c->resume), "%s", str);
     if (config_lookup_string(&cf, "CheckpointFile", &str)) snprintf(c->checkpoint, sizeof(c->checkpoint), "%s", str);
     config_lookup_int(&cf, "CheckpointEvery", &c->checkpoint_every);
+    config_lookup_int(&cf, "AutoTune", &c->autotune);
     {
         long long s;
         if (config_lookup_int64(&cf, "Seed", &s)) {
@@ -427,9 +431,10 @@ int main(int argc, char **argv)
                c.constrain_to_x, c.initial, c.eqm_steps, c.mega_steps, c.mc_moves, c.seed);
         printf("DisplayDumbTerminal %d\nCalculateRecombination %d\nCalculateRadialOrderParameter %d\n"
                "CalculatePotential %d\nCalculateEfield %d\nSaveDipolesXYZ %d\nSaveDipolesPNG %d\n"
-               "SaveDipolesSVG %d\nSavePotentialCube %d\nResumeFrom %s\nCheckpointFile %s\nCheckpointEvery %d\n",
+               "SaveDipolesSVG %d\nSavePotentialCube %d\nResumeFrom %s\nCheckpointFile %s\nCheckpointEvery %d\n"
+               "AutoTune %d\n",
                c.dumb_terminal, c.recombination, c.radial, c.potential, c.calc_efield, c.save_xyz, c.save_png,
-               c.save_svg, c.save_cube, c.resume, c.checkpoint, c.checkpoint_every);
+               c.save_svg, c.save_cube, c.resume, c.checkpoint, c.checkpoint_every, c.autotune);
         return 0;
     }
     {
@@ -469,6 +474,11 @@ int main(int argc, char **argv)
         }
         fprintf(a.log, "# Starrynight - simulation run on time(NULL)= %ld\n# Philox seed: %llX\n", (long)time(NULL),
                 c.seed);
+        if (c.autotune > 0) {
+            double ms = 0.0;
+            CK(sn_gpu_autotune(&P, &R, c.autotune, 5, R.block, &ms));
+            fprintf(stderr, "AutoTune: block %dx%dx%d, %.3f ms per sweep\n", R.block[0], R.block[1], R.block[2], ms);
+        }
         CK(sn_gpu_init(&P, 1, &R, &h));
         a.h = h;
         a.c = &c;

@@ -70,6 +70,13 @@ def test_lookups_are_type_strict_like_libconfig(tmp_path):
     assert v["T"] == "300"
 
 
+def test_autotune_key(tmp_path):
+    r, v = run(tmp_path, "AutoTune = 4\n")
+    assert r.returncode == 0 and v["AutoTune"] == "4"
+    r, v = run(tmp_path, "X = 8\n")
+    assert v["AutoTune"] == "0"
+
+
 def test_single_species_spelling(tmp_path):
     r, v = run(tmp_path, "Dipole = 1.5\nDipoleFraction = 0.7\nSeed = 99\n")
     assert v["Dipoles"] == "1.5 0" and v["Prevalence"] == "0.7 0.3" and v["Seed"] == "99"

@@ -38,3 +38,23 @@ def test_tune_table_once_per_size(native_lib):
             sim.init_lattice(i)
         acc, rej = sim.sweep(2, counts=True)
     assert acc + rej == 2 * (2 * 32 ** 3 + 48 ** 3)
+
+
+def test_native_autotuner_and_driver_key(native_lib, tmp_path):
+    """sn_gpu_autotune (the C-ABI tuner) returns one of the planner's candidates,
+    and the driver's AutoTune key runs with it."""
+    import subprocess
+    sn = native_lib
+    from starrynight_gb300 import autotune
+    params = sn.ModelParams(cutoff=3, dipoles=(1.0, 0.0), prevalence=(0.8, 0.2), seed=3)
+    rep = sn.Replica(48, 48, 48, T=200.0, seed=3)
+    shape, ms = autotune.tune_native(params, rep, max_candidates=3, sweeps=2)
+    cands = [(c["bx"], c["by"], c["bz"]) for c in sn.plan_candidates(48, 48, 48, 3, False, 3)]
+    assert shape in cands and ms > 0.0
+    cfg = ("T: 300\nX = 16\nY = 16\nZ = 16\nDipoles = [1.0, 0.0]\nPrevalence = [0.8, 0.2]\n"
+           "DipoleCutOff: 3\nMCEqmSteps: 1\nMCMegaSteps: 2\nMCMoves: 2.0\nAutoTune: 3\n")
+    (tmp_path / "starrynight.cfg").write_text(cfg)
+    r = subprocess.run([sn.driver_path()], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "AutoTune: block " in r.stderr
+    assert len([l for l in r.stdout.splitlines() if not l.startswith("#")]) == 2
