@@ -5,7 +5,9 @@ lattice by a model -- largest blocks that fit two CTAs per SM, least halo,
 conflict-free shared-memory strides.  ``tune`` times the top candidates on
 the GPU (CUDA events around whole sweeps, after warm-up) and returns the
 fastest shape; ``tune_table`` does so once per distinct lattice size of a
-replica table and returns the table with every replica's ``block`` set.
+replica table (optionally remembering choices in a JSON cache file) and
+returns the table with every replica's ``block`` set.  ``tune_native`` makes
+the same choice inside the C library (``sn_gpu_autotune``).
 
 A block shape changes the order in which sites are updated (every shape is
 an exact Metropolis sweep, so the physics is the same but trajectories
@@ -43,15 +45,35 @@ def tune(params: ModelParams, replica: Replica, max_candidates: int = 6, sweeps:
     return best, results
 
 
-def tune_table(params: ModelParams, replicas: Sequence[Replica], **kw) -> list:
-    """The table with each replica's block shape tuned (once per distinct size)."""
+def _cache_key(params: ModelParams, r: Replica) -> str:
+    return "%dx%dx%d/rc%d/%s" % (r.X, r.Y, r.Z, int(params.cutoff), "mixed" if _mixed(params) else "uniform")
+
+
+def tune_table(params: ModelParams, replicas: Sequence[Replica], cache: str | None = None, **kw) -> list:
+    """The table with each replica's block shape tuned (once per distinct size).
+
+    cache: a JSON file of earlier choices (lattice size, cutoff, mixed or
+    uniform lengths -> block shape) on this machine; sizes found there are
+    not timed again, new choices are added to it."""
+    import json
+    import os
+    known = {}
+    if cache and os.path.exists(cache):
+        with open(cache) as f:
+            known = {k: tuple(v) for k, v in json.load(f).items()}
     chosen = {}
     out = []
     for r in replicas:
-        key = (r.X, r.Y, r.Z)
+        key = _cache_key(params, r)
         if key not in chosen:
-            chosen[key] = tune(params, r, **kw)[0]
+            chosen[key] = known[key] if key in known else tune(params, r, **kw)[0]
         out.append(dataclasses.replace(r, block=chosen[key]))
+    if cache and any(k not in known for k in chosen):
+        known.update(chosen)
+        tmp = cache + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump({k: list(v) for k, v in sorted(known.items())}, f, indent=1)
+        os.replace(tmp, cache)
     return out
 
 
