@@ -25,6 +25,7 @@ typedef cudaError_t (*sn_flow_launch_fn)(bool two_d, bool mixed, const SnFlowArg
     cudaError_t sn_launch_sweep_rc##N(bool, bool, const SnPhaseArgs &, int, int, int, cudaStream_t);        \
     cudaError_t sn_launch_flow_rc##N(bool, bool, const SnFlowArgs &, int, int, int, cudaStream_t, int *);   \
     cudaError_t sn_launch_field_rc##N(bool, bool, bool, const void *, int, int, int, cudaStream_t);        \
+    cudaError_t sn_launch_field64_rc##N(bool, bool, const void *, int, int, int, cudaStream_t);            \
     void sn_geo_rc##N(bool, int *, int *, int *, int *, int *);
 SN_DECLARE_RC(1)
 SN_DECLARE_RC(2)

@@ -56,10 +56,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
     so = lib_path()
     if force or _stale(so, deps):
         jobs = []
-        for rc in range(1, MAX_CUTOFF + 1):
-            obj = os.path.join(LIBDIR, "sn_sweep_rc%d.o" % rc)
-            jobs.append([NVCC] + ARCH + NVFLAGS + ["-DSN_RC=%d" % rc, "-c", os.path.join(CSRC, "sn_sweep_inst.cu"),
-                                                   "-o", obj])
+        # per cutoff: the sweep kernels, the FP32-field pass and the FP64 pass
+        # as three objects, so the large stencils compile in parallel
+        for rc in range(MAX_CUTOFF, 0, -1):
+            for part in (1, 2, 3):
+                obj = os.path.join(LIBDIR, "sn_sweep_rc%d_p%d.o" % (rc, part))
+                jobs.append([NVCC] + ARCH + NVFLAGS + ["-DSN_RC=%d" % rc, "-DSN_PART=%d" % part, "-c",
+                                                       os.path.join(CSRC, "sn_sweep_inst.cu"), "-o", obj])
         for name in ("sn_kernels", "sn_gpu", "sn_noalloc", "sn_analysis"):
             jobs.append([NVCC] + ARCH + NVFLAGS + ["-c", os.path.join(CSRC, name + ".cu"),
                                                    "-o", os.path.join(LIBDIR, name + ".o")])
