@@ -61,7 +61,25 @@ typedef struct sn_params {
     float dipoles[SN_MAX_SPECIES];   /* Dipoles: species lengths (0 = vacancy)          */
     float prevalence[SN_MAX_SPECIES];/* Prevalence: species probabilities               */
     uint64_t seed;                   /* default Philox key for replicas with seed 0     */
+    int sweep_method;                /* SN_SWEEP_AUTO / _STENCIL / _CACHED (below)      */
 } sn_params;
+
+/* How the sweep forms a move's energy change (sn_params.sweep_method).  Both
+ * give the Metropolis sweep of site_energy (src/starrynight-montecarlo-core.c:
+ * 76-141); they differ in work and in the last bits of dE.
+ *   SN_SWEEP_STENCIL: every attempted move sums the cutoff stencil over the
+ *     neighbours' dipoles (the reference's way, on a shared-memory tile).
+ *   SN_SWEEP_CACHED: the local field of every site is kept in HBM as exact
+ *     fixed-point sums (each neighbour's contribution rounded to 2^-k on its
+ *     own, k about 20); an attempt reads it, an accepted move adds its
+ *     neighbours' changes.  Work per attempt no longer grows with the
+ *     cutoff, only per accepted move.  Needs every 3D block side >= 2 cutoff,
+ *     Z a multiple of 4 and dipoles with |components| <= 1; 2D replicas always
+ *     use the stencil.
+ *   SN_SWEEP_AUTO (0): CACHED where every 3D replica of the table admits it,
+ *     else STENCIL.  The environment variable SN_SWEEP=stencil|cached
+ *     overrides the choice. */
+enum { SN_SWEEP_AUTO = 0, SN_SWEEP_STENCIL = 1, SN_SWEEP_CACHED = 2 };
 
 /* One lattice of the replica table (batched mode: many per handle). */
 typedef struct sn_replica_desc {
@@ -95,6 +113,7 @@ typedef struct sn_schedule_info {
     int smem_bytes;        /* dynamic shared memory per block           */
     int merge;             /* 1: colour pairs c, c + (s/2,s/2,s/2)      */
     int threads;           /* threads per block of the sweep kernel     */
+    int field_cache;       /* 1: the cached-field sweep (SN_SWEEP_CACHED) */
 } sn_schedule_info;
 
 /* Initial lattice patterns (InitialLattice, src/starrynight-main.c:184-203). */
@@ -145,8 +164,20 @@ sn_status sn_gpu_download_lattice(sn_handle *h, int replica, float *xyz, float *
 /* n_sweeps Metropolis sweeps of every replica (each occupied site attempted
  * once per sweep), as CUDA-graph launches.  accept/reject (nullable) receive
  * the totals of this call over all replicas.  Replaces MC_moves(X*Y*Z*n)
- * (src/starrynight-montecarlo-core.c:143-191) and the ACCEPT/REJECT counters. */
+ * (src/starrynight-montecarlo-core.c:143-191) and the ACCEPT/REJECT counters.
+ * The call returns when its sweeps have finished on the GPU, with their own
+ * status: SN_ERR_TIMEOUT when a block of the dataflow schedule gave up
+ * waiting for a neighbour (sn_gpu_set_wait_limit).  The lattice is then not a
+ * valid Metropolis state: upload or initialise it again before sweeping on
+ * (the handle itself stays usable). */
 sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *reject);
+
+/* Polls a block of the dataflow sweep spends on one neighbour's done flag
+ * before it records SN_ERR_TIMEOUT and goes on (default 4194304 polls, about
+ * 1-4 s; >= 1).  Every device-side wait is bounded by it, so a sweep launch
+ * always ends.  The reference has no waits: it exit()s on its own errors
+ * (src/starrynight-config.c:113-121). */
+sn_status sn_gpu_set_wait_limit(sn_handle *h, uint32_t polls);
 
 /* sn_gpu_sweep, then the lattice of every replica r with xyz[r] != NULL
  * written to xyz[r] (3 floats per site, as sn_gpu_download_lattice with a
@@ -341,6 +372,25 @@ void *sn_gpu_stream(const sn_handle *h);
 sn_status sn_gpu_flow_stats(sn_handle *h, uint64_t *stats);
 sn_status sn_gpu_phase_times(sn_handle *h, int n_sweeps, double *avg_launch_ms, double *avg_sweep_ms,
                              int *launches_per_sweep);
+/* sn_gpu_sweep(h, n_sweeps, NULL, NULL) with *ms = the device time of those
+ * sweeps (CUDA events on the handle's stream around the graph launches and
+ * any periodic recompute, taken before the call's status read).
+ * Measurement hook; no reference counterpart. */
+sn_status sn_gpu_sweep_timed(sn_handle *h, int n_sweeps, double *ms);
+/* Checks the field cache of a replica that uses the cached-field sweep: the
+ * cache as the sweeps maintained it is compared with a fresh field-cache pass
+ * over the current lattice; *mismatches = differing int32 entries (0 when
+ * the incremental updates are exact, as designed).  The cache holds the
+ * fresh values afterwards.  SN_ERR_UNSUPPORTED for a stencil-sweep replica.
+ * Test and self-check hook; no reference counterpart. */
+sn_status sn_gpu_field_cache_check(sn_handle *h, int replica, uint64_t *mismatches);
+/* Test hook for the bounded waits: makes dataflow item `item` of the 3D
+ * variant wait, in every later sweep, on a flag that no block ever publishes
+ * (so that wait runs out and the sweep reports SN_ERR_TIMEOUT); item = -1
+ * restores the planned dependency list.  Nothing faults or hangs: the wait
+ * gives up after the limit of sn_gpu_set_wait_limit.  No reference
+ * counterpart. */
+sn_status sn_gpu_test_stall_block(sn_handle *h, int item);
 /* Measured FP32 FMA throughput of the current device (TFLOP/s, an FMA
  * counted as 2) and its nominal maximum SM clock; the roofline denominator
  * for the sweep kernel, which runs on CUDA cores. */

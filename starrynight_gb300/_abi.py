@@ -31,12 +31,16 @@ class SnError(RuntimeError):
         self.name = STATUS.get(status, str(status))
 
 
+SN_SWEEP_AUTO, SN_SWEEP_STENCIL, SN_SWEEP_CACHED = 0, 1, 2
+SWEEP_METHODS = {"auto": SN_SWEEP_AUTO, "stencil": SN_SWEEP_STENCIL, "cached": SN_SWEEP_CACHED}
+
+
 class Params(ctypes.Structure):
     _fields_ = [
         ("cutoff", ctypes.c_int), ("dim", ctypes.c_int), ("constrain_to_x", ctypes.c_int),
         ("cage_strain", ctypes.c_double), ("K", ctypes.c_double), ("efield", ctypes.c_float * 3),
         ("n_species", ctypes.c_int), ("dipoles", ctypes.c_float * SN_MAX_SPECIES),
-        ("prevalence", ctypes.c_float * SN_MAX_SPECIES), ("seed", ctypes.c_uint64),
+        ("prevalence", ctypes.c_float * SN_MAX_SPECIES), ("seed", ctypes.c_uint64), ("sweep_method", ctypes.c_int),
     ]
 
 
@@ -50,7 +54,8 @@ class ReplicaDesc(ctypes.Structure):
 
 class ScheduleInfo(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in ("bx", "by", "bz", "nbx", "nby", "nbz", "mx", "my", "mz", "s",
-                                             "halo", "tile_slots", "smem_bytes", "merge", "threads")]
+                                             "halo", "tile_slots", "smem_bytes", "merge", "threads",
+                                             "field_cache")]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -120,6 +125,10 @@ def lib() -> ctypes.CDLL:
             "sn_gpu_proposals": ([h, _i, _vp, _i, ctypes.c_uint32, _vp], _i),
             "sn_gpu_potential": ([h, _i, _i, _vp], _i),
             "sn_gpu_flow_stats": ([h, _vp], _i),
+            "sn_gpu_sweep_timed": ([h, _i, _P(ctypes.c_double)], _i),
+            "sn_gpu_set_wait_limit": ([h, ctypes.c_uint32], _i),
+            "sn_gpu_test_stall_block": ([h, _i], _i),
+            "sn_gpu_field_cache_check": ([h, _i, _P(ctypes.c_uint64)], _i),
             "sn_gpu_efield": ([h, _i, _i, _i, _vp], _i),
             "sn_gpu_radial_order": ([h, _i, _i, _vp, _vp, _vp], _i),
             "sn_gpu_order_parameters": ([h, _i, _P(ctypes.c_double), _P(ctypes.c_double), _vp], _i),

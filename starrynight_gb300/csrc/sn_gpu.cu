@@ -46,6 +46,13 @@ const sn_flow_launch_fn k_flow[SN_MAX_CUTOFF + 1] = {nullptr,
                                                       sn_launch_flow_rc5,
                                                       sn_launch_flow_rc6};
 
+const sn_cached_smem_fn k_cached_smem[SN_MAX_CUTOFF + 1] = {nullptr,            sn_cached_smem_rc1, sn_cached_smem_rc2,
+                                                             sn_cached_smem_rc3, sn_cached_smem_rc4, sn_cached_smem_rc5,
+                                                             sn_cached_smem_rc6};
+const sn_gfield_launch_fn k_gfield[SN_MAX_CUTOFF + 1] = {nullptr,            sn_launch_gfield_rc1, sn_launch_gfield_rc2,
+                                                         sn_launch_gfield_rc3, sn_launch_gfield_rc4, sn_launch_gfield_rc5,
+                                                         sn_launch_gfield_rc6};
+
 const int kSmemLimit = 227 * 1024;
 
 // Unique key of block (bx, by, bz) of replica rep (block indices < 2^14 per axis: the
@@ -71,6 +78,11 @@ struct SnPlan {
 
 int block_colour(const SnTile &t, const int *c) { return (c[0] % t.m[0]) * 4 + (c[1] % t.m[1]) * 2 + (c[2] % t.m[2]); }
 
+// Dynamic shared memory and threads of the sweep kernel that runs replica
+// tile t: the cached-field kernel (t.cmode) or the stencil kernel.
+int sweep_smem(const SnTile &t) { return t.cmode ? t.csmem : t.smem_bytes; }
+int sweep_threads(const SnTile &t) { return t.cmode ? SN_CACHED_THREADS : t.threads; }
+
 bool build_plan(const std::vector<SnTile> &tiles, const sn_replica_desc *replicas, int n, bool flow, SnPlan &pl,
                 std::string &why, int ready = 512)
 {
@@ -92,8 +104,8 @@ bool build_plan(const std::vector<SnTile> &tiles, const sn_replica_desc *replica
                         for (int bz = 0; bz < t.nb[2]; bz++) {
                             if (bx % t.m[0] != cb[0] || by % t.m[1] != cb[1] || bz % t.m[2] != cb[2]) continue;
                             work.push_back(SnWork{r, bx * t.B[0], by * t.B[1], bz * t.B[2]});
-                            pl.work_smem[k] = std::max(pl.work_smem[k], t.smem_bytes);
-                            pl.work_thr[k] = std::max(pl.work_thr[k], t.threads);
+                            pl.work_smem[k] = std::max(pl.work_smem[k], sweep_smem(t));
+                            pl.work_thr[k] = std::max(pl.work_thr[k], sweep_threads(t));
                         }
             }
             pl.work_cnt[k] = (int)work.size() - pl.work_off[k];
@@ -283,10 +295,37 @@ std::vector<int> block_candidates(int L, int rc)
     return c;
 }
 
+// Geometry of the cached-field sweep for t's block shape (t.cmode = 1), or
+// false when the shape does not admit it: every block side >= 2 cutoff (tiles
+// of blocks that may run together are then disjoint), Z and the z side
+// multiples of 4 (16-byte tile rows), at most SN_CACHED_THREADS targets per
+// colour group, and a tile that fits `limit` bytes with >= pc_min groups of
+// proposals staged.
+bool plan_cached(SnTile &t, int Z, int rc, bool mixed, int limit, int pc_min)
+{
+    if (Z == 1 || Z % 4 || t.B[2] % 4) return false;
+    for (int a = 0; a < 3; a++)
+        if (t.B[a] < 2 * rc) return false;
+    if (t.tg > SN_CACHED_THREADS) return false;
+    t.cH[0] = rc;
+    t.cH[1] = rc;
+    t.cH[2] = (rc + 3) / 4 * 4;
+    for (int a = 0; a < 3; a++) t.cT[a] = t.B[a] + 2 * t.cH[a];
+    t.cslots = t.cT[0] * t.cT[1] * t.cT[2];
+    t.cpc = t.ng;
+    while (t.cpc > 1 && k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed) > limit) t.cpc--;
+    t.csmem = k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed);
+    if (t.csmem > limit || t.cpc < pc_min) return false;
+    if (sn_sweep::sn_gfield_smem(t.cslots, mixed) > kSmemLimit) return false;
+    t.cmode = 1;
+    return true;
+}
+
 // Feasible tile plans of an X x Y x Z replica in preference order (at most
-// max_out; force = a block shape to use instead of choosing).
+// max_out; force = a block shape to use instead of choosing); cached: plans
+// for the cached-field sweep only.
 bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &outs, size_t max_out, std::string &why,
-                const int *force_shape = nullptr)
+                const int *force_shape = nullptr, bool cached = false)
 {
     if (rc < 1 || rc > SN_MAX_CUTOFF) {
         why = "cutoff outside 1.." + std::to_string(SN_MAX_CUTOFF);
@@ -326,6 +365,7 @@ bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &ou
         for (int by : cands[1])
             for (int bz : cands[2]) {
                 if (force[0] && (bx != force[0] || by != force[1] || bz != force[2])) continue;
+                if (cached && (two_d || bx < 2 * rc || by < 2 * rc || bz < 2 * rc || bz % 4 || Z % 4)) continue;
                 Cand c{{bx, by, bz}, (long long)bx * by * bz, 0};
                 c.balanced = (bx % S == 0) + (by % S == 0) + (two_d || bz % S == 0);
                 all.push_back(c);
@@ -348,7 +388,10 @@ bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &ou
     // barriers then overlap the other's work: measured faster at 256^3);
     // pass 1 takes the largest shape that fits one block per SM.
     for (int pass = 0; pass < 2; pass++) {
-        const int limit = pass == 0 ? kSmemTwoPerSm : kSmemLimit - kSweepStatic;
+        const int pass_limit = pass == 0 ? kSmemTwoPerSm : kSmemLimit - kSweepStatic;
+        // the stencil tile (sweep and field pass); with the cached sweep only
+        // the field pass uses it, which may take a whole SM
+        const int limit = cached ? kSmemLimit - kSweepStatic : pass_limit;
         for (const Cand &c : all) {
             SnTile t;
             memset(&t, 0, sizeof(t));
@@ -366,8 +409,8 @@ bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &ou
             t.threads = NS * t.tg;
             t.ng = ng;
             t.merge = merge;
-            if (t.threads > (pass == 0 ? SN_TWO_PER_SM_THREADS : SN_SWEEP_MAX_THREADS)) continue;
-            const int pc_min = pass == 0 ? std::min(8, ng) : 1;
+            if (t.threads > (pass == 0 && !cached ? SN_TWO_PER_SM_THREADS : SN_SWEEP_MAX_THREADS)) continue;
+            const int pc_min = pass == 0 && !cached ? std::min(8, ng) : 1;
             // quick lower bound on shared memory with no padding
             if ((int)sn_sweep::sn_carve(t.T[0] * t.T[1] * t.T[2], t.tg, pc_min, NS, S, NF, mixed, 4).total > limit)
                 continue;
@@ -397,6 +440,8 @@ bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &ou
             t.smem_bytes = (int)sn_sweep::sn_carve(t.slots, t.tg, t.pc, NS, S, NF, mixed, 4).total;
             t.field_smem = (int)sn_sweep::sn_carve(t.slots, t.tg, 0, NS, S, NF, mixed, 8).total;
             if (t.smem_bytes > limit || t.field_smem > kSmemLimit || t.pc < pc_min) continue;
+            if (cached && !plan_cached(t, Z, rc, mixed, pass_limit - kSweepStatic, pass == 0 ? std::min(8, ng) : 1))
+                continue;
             bool seen = false;  // pass 1 meets pass 0's shapes again
             for (const SnTile &o : outs) seen |= o.B[0] == t.B[0] && o.B[1] == t.B[1] && o.B[2] == t.B[2];
             if (seen) continue;
@@ -414,12 +459,94 @@ bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &ou
     return false;
 }
 
-bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string &why, const int *force = nullptr)
+bool plan_tile(int X, int Y, int Z, int rc, bool mixed, SnTile &out, std::string &why, const int *force = nullptr,
+               bool cached = false)
 {
     std::vector<SnTile> v;
-    if (!plan_tiles(X, Y, Z, rc, mixed, v, 1, why, force)) return false;
+    if (!plan_tiles(X, Y, Z, rc, mixed, v, 1, why, force, cached)) return false;
     out = v[0];
     return true;
+}
+
+// The sweep method a table asks for: sn_params.sweep_method, overridden by
+// the environment variable SN_SWEEP=stencil|cached.
+int sweep_method(const sn_params &P)
+{
+    if (const char *env = getenv("SN_SWEEP")) {
+        if (!strcmp(env, "stencil")) return SN_SWEEP_STENCIL;
+        if (!strcmp(env, "cached")) return SN_SWEEP_CACHED;
+    }
+    return P.sweep_method;
+}
+
+// Tiles of every replica of a table.  The 3D replicas all take the cached-
+// field sweep (auto: when every one of them admits it) or all the stencil
+// sweep; 2D replicas always take the stencil sweep.  *cached = the choice.
+bool plan_table(const sn_params &P, int n, const sn_replica_desc *replicas, bool mixed, std::vector<SnTile> &tiles,
+                bool *cached, std::string &why)
+{
+    const int method = sweep_method(P);
+    if (method != SN_SWEEP_AUTO && method != SN_SWEEP_STENCIL && method != SN_SWEEP_CACHED) {
+        why = "unknown sweep_method " + std::to_string(method);
+        return false;
+    }
+    tiles.assign(n, SnTile{});
+    bool use = method != SN_SWEEP_STENCIL;
+    for (int r = 0; r < n && use; r++) {
+        const sn_replica_desc &d = replicas[r];
+        if (d.Z == 1) continue;
+        std::string w;
+        if (!plan_tile(d.X, d.Y, d.Z, P.cutoff, mixed, tiles[r], w, d.block, true)) {
+            if (method == SN_SWEEP_CACHED) {
+                why = "replica " + std::to_string(r) + " (" + std::to_string(d.X) + "x" + std::to_string(d.Y) + "x" +
+                      std::to_string(d.Z) + "): no block shape for the cached-field sweep (block sides >= 2 cutoff, "
+                      "Z and bz multiples of 4, tile in shared memory)";
+                return false;
+            }
+            use = false;
+        }
+    }
+    for (int r = 0; r < n; r++) {
+        const sn_replica_desc &d = replicas[r];
+        if (use && d.Z > 1) continue;
+        std::string w;
+        if (!plan_tile(d.X, d.Y, d.Z, P.cutoff, mixed, tiles[r], w, d.block, false)) {
+            why = "replica " + std::to_string(r) + " (" + std::to_string(d.X) + "x" + std::to_string(d.Y) + "x" +
+                  std::to_string(d.Z) + "): " + w;
+            return false;
+        }
+    }
+    *cached = use && std::any_of(replicas, replicas + n, [](const sn_replica_desc &d) { return d.Z > 1; });
+    return true;
+}
+
+// Power-of-two scale 2^k of the field cache: every contribution satisfies
+// |c| 2^k < 2^22 (the rounding of q_bits) and every field |g| 2^k < 2^30,
+// for dipole components |p| <= 1.0001 (checked at upload) and lengths up to
+// Lmax.  The bounds take each offset tensor's largest row sum.
+int cache_scale(int rc, double Lmax, double C)
+{
+    double vmax = 0.0, gsum = 0.0;
+    for (int x = -rc; x <= rc; x++)
+        for (int y = -rc; y <= rc; y++)
+            for (int z = -rc; z <= rc; z++) {
+                const int r2 = x * x + y * y + z * z;
+                if (r2 == 0 || r2 > rc * rc) continue;
+                const double d = std::sqrt((double)r2), i3 = 1.0 / (r2 * d), i5 = i3 / r2;
+                const int o[3] = {x, y, z};
+                double row = 0.0;
+                for (int a = 0; a < 3; a++) {
+                    double s = 0.0;
+                    for (int b = 0; b < 3; b++) s += std::fabs((a == b ? i3 : 0.0) - 3.0 * o[a] * o[b] * i5);
+                    row = std::max(row, s);
+                }
+                const double v = (Lmax * Lmax * row + (r2 == 1 ? std::fabs(C) : 0.0)) * 1.0002;
+                vmax = std::max(vmax, v);
+                gsum += v;
+            }
+    int k = 30;
+    while (k > 0 && (std::ldexp(vmax, k) >= 4194304.0 || std::ldexp(gsum, k) >= 1073741824.0)) k--;
+    return k;
 }
 
 void fill_info(const SnTile &t, int rc, sn_schedule_info *o)
@@ -438,7 +565,12 @@ void fill_info(const SnTile &t, int rc, sn_schedule_info *o)
     o->tile_slots = t.slots;
     o->smem_bytes = t.smem_bytes;
     o->merge = t.merge;
-    o->threads = t.threads;
+    o->threads = t.cmode ? SN_CACHED_THREADS : t.threads;
+    o->field_cache = t.cmode;
+    if (t.cmode) {
+        o->tile_slots = t.cslots;
+        o->smem_bytes = t.csmem;
+    }
 }
 
 }  // namespace
@@ -503,8 +635,13 @@ struct sn_handle {
     uint32_t *d_done = nullptr;
     size_t done_n = 0;
     uint32_t *d_queue = nullptr;  // 2 counters
-    uint32_t *d_err = nullptr;    // timeout flag, stall statistics
+    uint32_t *d_err = nullptr;    // timeout flag, stall statistics, poll limit (SnFlowArgs::err)
+    std::vector<int> deps_host;   // the dataflow lists as planned (a test hook edits one on the device)
+    int stalled_item = -1;        // item whose first dependency points at the spare flag, or -1
     std::vector<float *> lattice_mem;
+    // cached-field sweep of the 3D replicas: their field caches (3N int32 each)
+    bool cached = false;
+    std::vector<int *> gcache_mem;
     // scratch (lazy)
     float *d_stage = nullptr;
     size_t stage_floats = 0;
@@ -582,7 +719,23 @@ SnFieldArgsHost field_args(sn_handle *h, int r, double *site_e, float *grad, dou
     a.grad = grad;
     a.red = red;
     a.red_stride = stride;
+    a.write_g = 0;
     return a;
+}
+
+// Field-cache pass (exact fixed-point g and the energy sums) over the blocks
+// bx in [b0, b1) of replica r, which must hold a field cache.
+sn_status launch_gfield_x(sn_handle *h, int r, const SnFieldArgsHost &base, int b0, int b1, cudaStream_t st)
+{
+    if (b1 <= b0) return SN_OK;
+    const SnTile &t = h->tiles[r];
+    SnFieldArgsHost a = base;
+    a.write_g = 1;
+    a.work = base.work + (size_t)b0 * t.nb[1] * t.nb[2];
+    SN_CK(h, k_gfield[h->rc](h->mixed, &a, (b1 - b0) * t.nb[1] * t.nb[2], sn_sweep::sn_gfield_smem(t.cslots, h->mixed),
+                             st));
+    h->launches++;
+    return SN_OK;
 }
 
 sn_status launch_field(sn_handle *h, int r, bool fp64, const SnFieldArgsHost &a)
@@ -608,13 +761,18 @@ sn_status launch_field_x(sn_handle *h, int r, const SnFieldArgsHost &base, int b
     return SN_OK;
 }
 
-// Recompute replica r's running E and P from a full field pass.
+// Recompute replica r's running E and P from a full field pass.  A replica
+// with a field cache whose dipoles changed outside the sweep (record = 0:
+// initialisation, quench, field change) gets its cache rebuilt by the same
+// pass; the periodic drift checks (record = 1) leave the cache alone.
 sn_status recompute_one(sn_handle *h, int r, int prec, int record)
 {
     double *red = h->d_red + 10 * r;
     SN_CK(h, cudaMemsetAsync(red, 0, 10 * sizeof(double), h->stream));
     SnFieldArgsHost a = field_args(h, r, nullptr, nullptr, h->d_red, 10);
-    sn_status s = launch_field(h, r, prec == SN_ENERGY_FP64, a);
+    const bool gpass = h->tiles[r].cmode && !record && prec == SN_ENERGY_FP32;
+    sn_status s = gpass ? launch_gfield_x(h, r, a, 0, h->tiles[r].nb[0], h->stream)
+                        : launch_field(h, r, prec == SN_ENERGY_FP64, a);
     if (s) return s;
     SN_CK(h, sn_launch_recompute_finish(red, h->d_state, h->d_reps, r, h->params.cage_strain, h->d_drift, record,
                                         h->stream));
@@ -661,8 +819,8 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
             }
             if (events && ev + 1 < events->size()) e = cudaEventRecord((*events)[ev++], h->stream);
             if (e == cudaSuccess)
-                e = k_flow[h->rc](v == 1, h->mixed, f, std::min(h->flow_grid[v], h->flow_items[v]), thr, smem,
-                                  h->stream, nullptr);
+                e = k_flow[h->rc](v == 1, h->mixed, h->cached && v == 0, f, std::min(h->flow_grid[v], h->flow_items[v]),
+                                  thr, smem, h->stream, nullptr);
             if (events && ev < events->size() && e == cudaSuccess) e = cudaEventRecord((*events)[ev++], h->stream);
             if (nodes) (*nodes)++;
         }
@@ -679,7 +837,9 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
             if (!h->work_cnt[k]) continue;
             const SnPhaseArgs a = phase_args(h, h->work_off[k], h->work_cnt[k]);
             if (events && ev + 1 < events->size()) e = cudaEventRecord((*events)[ev++], h->stream);
-            if (e == cudaSuccess) e = k_sweep[h->rc](v == 1, h->mixed, a, h->work_cnt[k], h->work_thr[k], h->work_smem[k], h->stream);
+            if (e == cudaSuccess)
+                e = k_sweep[h->rc](v == 1, h->mixed, h->cached && v == 0, a, h->work_cnt[k], h->work_thr[k],
+                                   h->work_smem[k], h->stream);
             if (events && ev < events->size() && e == cudaSuccess) e = cudaEventRecord((*events)[ev++], h->stream);
             if (nodes) (*nodes)++;
         }
@@ -707,14 +867,15 @@ sn_status capture_graph(sn_handle *h)
 {
     // configure function attributes (and size the dataflow grid) outside the capture
     for (int v = 0; v < 2; v++) {
-        SN_CK(h, k_sweep[h->rc](v == 1, h->mixed, SnPhaseArgs{}, 0, 0, 0, h->stream));
+        SN_CK(h, k_sweep[h->rc](v == 1, h->mixed, h->cached && v == 0, SnPhaseArgs{}, 0, 0, 0, h->stream));
         if (h->flow && h->flow_items[v]) {
             int thr = 0, smem = 0;
             for (int p = 0; p < 8; p++) {
                 thr = std::max(thr, h->work_thr[p * 2 + v]);
                 smem = std::max(smem, h->work_smem[p * 2 + v]);
             }
-            SN_CK(h, k_flow[h->rc](v == 1, h->mixed, SnFlowArgs{}, 0, thr, smem, h->stream, &h->flow_grid[v]));
+            SN_CK(h, k_flow[h->rc](v == 1, h->mixed, h->cached && v == 0, SnFlowArgs{}, 0, thr, smem, h->stream,
+                                   &h->flow_grid[v]));
             if (h->flow_grid[v] < 1) return fail(h, SN_ERR_CUDA, "dataflow kernel cannot be resident");
         }
     }
@@ -738,6 +899,7 @@ void destroy_all(sn_handle *h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     for (float *p : h->lattice_mem) cudaFree(p);
+    for (int *p : h->gcache_mem) cudaFree(p);
     void *ptrs[] = {h->d_reps,  h->d_geoms, h->d_acc,   h->d_state, h->d_sweep, h->d_hist, h->d_red,
                     h->d_drift, h->d_ex,    h->d_order, h->d_flags, h->d_work,  h->d_stage, h->d_site,
                     h->d_grad,  h->d_trace, h->d_deps,  h->d_done,  h->d_queue, h->d_err,
@@ -802,7 +964,17 @@ sn_status sn_plan_schedule(int X, int Y, int Z, int cutoff, int mixed_lengths, s
     std::string why;
     if (cutoff < 1 || cutoff > SN_MAX_CUTOFF)
         return fail(nullptr, SN_ERR_UNSUPPORTED, "cutoff %d outside 1..%d", cutoff, SN_MAX_CUTOFF);
-    if (!plan_tile(X, Y, Z, cutoff, mixed_lengths != 0, t, why)) return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
+    sn_params P{};
+    P.cutoff = cutoff;
+    sn_replica_desc d{};
+    d.X = X;
+    d.Y = Y;
+    d.Z = Z;
+    std::vector<SnTile> tiles;
+    bool cached = false;
+    if (!plan_table(P, 1, &d, mixed_lengths != 0, tiles, &cached, why))
+        return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
+    t = tiles[0];
     fill_info(t, cutoff, out);
     return SN_OK;
 }
@@ -820,11 +992,11 @@ sn_status sn_check_flow(const sn_params *params, int n_replicas, const sn_replic
             if (L == 0.0f) L = P.dipoles[i];
             else if (P.dipoles[i] != L) mixed = true;
         }
-    std::vector<SnTile> tiles(n_replicas);
+    std::vector<SnTile> tiles;
     std::string why;
-    for (int r = 0; r < n_replicas; r++)
-        if (!plan_tile(replicas[r].X, replicas[r].Y, replicas[r].Z, P.cutoff, mixed, tiles[r], why, replicas[r].block))
-            return fail(nullptr, SN_ERR_SCHEDULE, "replica %d: %s", r, why.c_str());
+    bool cached = false;
+    if (!plan_table(P, n_replicas, replicas, mixed, tiles, &cached, why))
+        return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
     SnPlan pl;
     if (!build_plan(tiles, replicas, n_replicas, true, pl, why)) return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
     // Independent check of the dataflow lists (direct block grids, not the key map):
@@ -895,8 +1067,14 @@ sn_status sn_plan_candidates(int X, int Y, int Z, int cutoff, int mixed_lengths,
     std::vector<SnTile> v;
     std::string why;
     *n_out = 0;
-    if (!plan_tiles(X, Y, Z, cutoff, mixed_lengths != 0, v, (size_t)max_out, why))
-        return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
+    // the default method's candidates: the cached-field sweep's where the lattice admits it
+    sn_params P{};
+    const bool try_cached = Z > 1 && sweep_method(P) != SN_SWEEP_STENCIL;
+    if (!(try_cached && plan_tiles(X, Y, Z, cutoff, mixed_lengths != 0, v, (size_t)max_out, why, nullptr, true))) {
+        v.clear();
+        if (!plan_tiles(X, Y, Z, cutoff, mixed_lengths != 0, v, (size_t)max_out, why))
+            return fail(nullptr, SN_ERR_SCHEDULE, "%s", why.c_str());
+    }
     for (size_t i = 0; i < v.size(); i++) fill_info(v[i], cutoff, &out[i]);
     *n_out = (int)v.size();
     return SN_OK;
@@ -1061,11 +1239,20 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(h, SN_ERR_CUDA, "cudaEventCreate failed"));
 
-    for (int r = 0; r < n_replicas; r++) {
+    {
         std::string why;
+        if (!plan_table(P, n_replicas, replicas, mixed, h->tiles, &h->cached, why))
+            return bail(fail(h, SN_ERR_SCHEDULE, "%s", why.c_str()));
+    }
+    float Lmax = 0.0f;
+    for (int i = 0; i < P.n_species; i++) Lmax = std::max(Lmax, P.dipoles[i]);
+    const int gk = h->cached ? cache_scale(P.cutoff, (double)Lmax, P.cage_strain) : 0;
+    if (h->cached && gk < 8)
+        return bail(fail(h, SN_ERR_CONFIG, "the cached-field sweep's fixed point has too few bits (k = %d) for "
+                                           "Dipoles up to %g and CageStrain %g: use SN_SWEEP_STENCIL", gk,
+                         (double)Lmax, P.cage_strain));
+    for (int r = 0; r < n_replicas; r++) {
         const sn_replica_desc &d = replicas[r];
-        if (!plan_tile(d.X, d.Y, d.Z, P.cutoff, mixed, h->tiles[r], why, d.block))
-            return bail(fail(h, SN_ERR_SCHEDULE, "replica %d (%dx%dx%d): %s", r, d.X, d.Y, d.Z, why.c_str()));
         const long long N = (long long)d.X * d.Y * d.Z;
         float *mem = nullptr;
         if (cudaMalloc(&mem, 4 * N * sizeof(float)) != cudaSuccess)
@@ -1091,6 +1278,17 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         const uint64_t seed = d.seed ? d.seed : P.seed + (uint64_t)r;
         R.seed_lo = (uint32_t)seed;
         R.seed_hi = (uint32_t)(seed >> 32);
+        if (h->tiles[r].cmode) {
+            int *gc = nullptr;
+            if (cudaMalloc(&gc, 3 * (size_t)N * sizeof(int)) != cudaSuccess)
+                return bail(fail(h, SN_ERR_NOMEM, "replica %d: cannot allocate the field cache of %lld sites", r, N));
+            h->gcache_mem.push_back(gc);
+            if (cudaMemsetAsync(gc, 0, 3 * (size_t)N * sizeof(int), h->stream) != cudaSuccess)
+                return bail(fail(h, SN_ERR_CUDA, "cudaMemset failed"));
+            R.gcache = gc;
+            R.gscale = std::ldexp(1.0f, gk);
+            R.ginv = std::ldexp(1.0f, -gk);
+        }
     }
 
     if (const char *env = getenv("SN_SCHEDULE")) h->flow = strcmp(env, "phases") != 0;
@@ -1144,7 +1342,8 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     ALLOC(h->d_work, std::max<size_t>(work.size(), 1) * sizeof(SnWork));
     if (h->flow) {
         ALLOC(h->d_deps, deps.size() * sizeof(int));
-        ALLOC(h->d_done, work.size() * sizeof(uint32_t));
+        // one spare flag past the last item: never published (sn_gpu_test_stall_block)
+        ALLOC(h->d_done, (work.size() + 1) * sizeof(uint32_t));
         h->done_n = work.size();
         ALLOC(h->d_queue, 2 * sizeof(uint32_t));
         ALLOC(h->d_err, 4 * sizeof(uint32_t));
@@ -1161,6 +1360,10 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_order, order.data(), nr * sizeof(int), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess && h->flow)
         e = cudaMemcpyAsync(h->d_deps, deps.data(), deps.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    const uint32_t wait_limit = SN_WAIT_LIMIT_DEFAULT;
+    if (e == cudaSuccess && h->flow)
+        e = cudaMemcpyAsync(h->d_err + 3, &wait_limit, sizeof(wait_limit), cudaMemcpyHostToDevice, h->stream);
+    if (h->flow) h->deps_host = deps;
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->d_ex, &ex, sizeof(ex), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return bail(fail(h, SN_ERR_CUDA, "init upload: %s", cudaGetErrorString(e)));
@@ -1256,14 +1459,17 @@ sn_status sn_gpu_upload_lattice(sn_handle *h, int replica, const float *xyz, con
         // blocks whose tile x range [b*Bx - H, (b+1)*Bx + H) lies in [0, x1)
         int last = (x1 - H) / Bx - 1;
         if (q == Q - 1) last = nb - 1;
-        if ((s = launch_field_x(h, replica, fa, next_b, last + 1, fs))) return s;
+        if ((s = t.cmode ? launch_gfield_x(h, replica, fa, next_b, last + 1, fs)
+                         : launch_field_x(h, replica, fa, next_b, last + 1, fs)))
+            return s;
         next_b = std::max(next_b, last + 1);
     }
     for (int k = 0; k < 2; k++) {
         SN_CK(h, cudaEventRecord(h->fdone_ev[k], h->field_stream[k]));
         SN_CK(h, cudaStreamWaitEvent(h->stream, h->fdone_ev[k], 0));
     }
-    if ((s = launch_field_x(h, replica, fa, 0, 1, h->stream))) return s;
+    if ((s = t.cmode ? launch_gfield_x(h, replica, fa, 0, 1, h->stream) : launch_field_x(h, replica, fa, 0, 1, h->stream)))
+        return s;
     SN_CK(h, sn_launch_recompute_finish(red, h->d_state, h->d_reps, replica, h->params.cage_strain, h->d_drift, 0,
                                         h->stream));
     h->launches++;
@@ -1271,6 +1477,9 @@ sn_status sn_gpu_upload_lattice(sn_handle *h, int replica, const float *xyz, con
     SN_CK(h, cudaMemcpyAsync(flags, h->d_flags, sizeof(flags), cudaMemcpyDeviceToHost, h->stream));
     SN_CK(h, cudaStreamSynchronize(h->stream));
     if (flags[2]) return fail(h, SN_ERR_ARG, "negative or non-finite dipole length in upload");
+    if (flags[3] && t.cmode)
+        return fail(h, SN_ERR_ARG, "upload has a dipole component beyond +-1; the cached-field sweep (SN_SWEEP_CACHED, "
+                                   "the default where it applies) needs unit or shorter dipoles: use SN_SWEEP_STENCIL");
     if (flags[0])
         return fail(h, SN_ERR_ARG, "upload has a dipole length other than %g, but the handle was created for a single "
                                    "species length (list every species in sn_params.dipoles)", (double)h->length);
@@ -1321,7 +1530,8 @@ float *device_view(float *p, size_t n)
 // n sweeps; outs (nrep entries, nullable) are device views that the last
 // sweep writes its final sites to.  Every pointer set here is cleared again
 // before returning, also on failure.
-sn_status run_sweeps(sn_handle *h, int n_sweeps, float *const *outs, uint64_t *accept, uint64_t *reject)
+sn_status run_sweeps(sn_handle *h, int n_sweeps, float *const *outs, uint64_t *accept, uint64_t *reject,
+                     cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr)
 {
     std::vector<SnState> before;
     if (accept || reject) {
@@ -1335,6 +1545,7 @@ sn_status run_sweeps(sn_handle *h, int n_sweeps, float *const *outs, uint64_t *a
             if (outs[r]) sn_launch_set_out(h->d_reps, r, nullptr, h->stream);
         armed = false;
     };
+    if (ev_begin) SN_CK(h, cudaEventRecord(ev_begin, h->stream));
     for (int i = 0; i < n_sweeps; i++) {
         if (outs && i == n_sweeps - 1) {
             armed = true;
@@ -1361,6 +1572,9 @@ sn_status run_sweeps(sn_handle *h, int n_sweeps, float *const *outs, uint64_t *a
         h->launches += h->graph_nodes;
         h->sweeps++;
         if (h->recompute_every > 0 && h->sweeps % (uint64_t)h->recompute_every == 0) {
+            // a drift check of a lattice whose sweep gave up a wait would be meaningless
+            sn_status s = flow_status(h);
+            if (s) return s;
             for (int r = 0; r < h->nrep; r++) {
                 sn_status s = recompute_one(h, r, h->recompute_prec, 1);
                 if (s) return s;
@@ -1368,6 +1582,7 @@ sn_status run_sweeps(sn_handle *h, int n_sweeps, float *const *outs, uint64_t *a
             h->n_checks++;
         }
     }
+    if (ev_end) SN_CK(h, cudaEventRecord(ev_end, h->stream));
     if (accept || reject) {
         std::vector<SnState> after(h->nrep);
         SN_CK(h, cudaMemcpyAsync(after.data(), h->d_state, h->nrep * sizeof(SnState), cudaMemcpyDeviceToHost, h->stream));
@@ -1379,9 +1594,10 @@ sn_status run_sweeps(sn_handle *h, int n_sweeps, float *const *outs, uint64_t *a
         }
         if (accept) *accept = a;
         if (reject) *reject = t - a;
-        sn_status s = flow_status(h);
-        if (s) return s;
     }
+    // every call reports its own sweeps' waits (this synchronises the stream)
+    sn_status s = flow_status(h);
+    if (s) return s;
     SN_CK(h, cudaGetLastError());
     return SN_OK;
 }
@@ -1393,6 +1609,90 @@ sn_status sn_gpu_sweep(sn_handle *h, int n_sweeps, uint64_t *accept, uint64_t *r
     if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
     if (n_sweeps < 0) return fail(h, SN_ERR_ARG, "negative sweep count");
     return run_sweeps(h, n_sweeps, nullptr, accept, reject);
+}
+
+sn_status sn_gpu_sweep_timed(sn_handle *h, int n_sweeps, double *ms)
+{
+    if (!h || !ms) return fail(h, SN_ERR_ARG, "null handle or output");
+    if (n_sweeps < 1) return fail(h, SN_ERR_ARG, "need n_sweeps >= 1");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SN_CK(h, cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(h, SN_ERR_CUDA, "cudaEventCreate failed");
+    }
+    sn_status s = run_sweeps(h, n_sweeps, nullptr, nullptr, nullptr, e0, e1);
+    float t = 0.0f;
+    if (!s && cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) s = fail(h, SN_ERR_CUDA, "cudaEventElapsedTime failed");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!s) *ms = t;
+    return s;
+}
+
+sn_status sn_gpu_set_wait_limit(sn_handle *h, uint32_t polls)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    if (polls < 1) return fail(h, SN_ERR_ARG, "the poll limit must be >= 1");
+    if (!h->flow) return SN_OK;  // the eight-launch schedule never waits
+    SN_CK(h, cudaMemcpyAsync(h->d_err + 3, &polls, sizeof(polls), cudaMemcpyHostToDevice, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    return SN_OK;
+}
+
+sn_status sn_gpu_field_cache_check(sn_handle *h, int replica, uint64_t *mismatches)
+{
+    sn_status s = check_rep(h, replica);
+    if (s) return s;
+    if (!mismatches) return fail(h, SN_ERR_ARG, "null output");
+    const SnReplicaDev &R = h->reps[replica];
+    if (!R.gcache) return fail(h, SN_ERR_UNSUPPORTED, "replica %d has no field cache (stencil sweep)", replica);
+    const size_t n3 = 3 * (size_t)R.n_sites;
+    // the cache as the sweeps left it, then a fresh field-cache pass over it, then compare
+    s = ensure(h, (void **)&h->d_site, &h->site_n, (n3 + 1) / 2 + 1, sizeof(double));
+    if (s) return s;
+    int *old = reinterpret_cast<int *>(h->d_site);
+    unsigned long long *cnt = reinterpret_cast<unsigned long long *>(h->d_site + (n3 + 1) / 2);
+    SN_CK(h, cudaMemcpyAsync(old, R.gcache, n3 * sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
+    SN_CK(h, cudaMemsetAsync(cnt, 0, sizeof(*cnt), h->stream));
+    SnFieldArgsHost a = field_args(h, replica, nullptr, nullptr, nullptr, 0);
+    if ((s = launch_gfield_x(h, replica, a, 0, h->tiles[replica].nb[0], h->stream))) return s;
+    SN_CK(h, sn_launch_count_diff(old, R.gcache, (long long)n3, cnt, h->stream));
+    h->launches++;
+    unsigned long long c = 0;
+    SN_CK(h, cudaMemcpyAsync(&c, cnt, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    SN_CK(h, cudaStreamSynchronize(h->stream));
+    *mismatches = c;
+    return SN_OK;
+}
+
+sn_status sn_gpu_test_stall_block(sn_handle *h, int item)
+{
+    if (!h) return fail(nullptr, SN_ERR_ARG, "null handle");
+    if (!h->flow) return fail(h, SN_ERR_UNSUPPORTED, "the eight-launch schedule has no dependency waits");
+    const int n3d = h->flow_items[0];
+    if (item < -1 || item >= n3d) return fail(h, SN_ERR_ARG, "item %d outside the 3D dataflow list [0,%d)", item, n3d);
+    auto put = [&](int k, const int *v) -> sn_status {
+        SN_CK(h, cudaMemcpyAsync(h->d_deps + (size_t)(h->flow_off[0] + k) * SN_MAX_DEPS, v, SN_MAX_DEPS * sizeof(int),
+                                 cudaMemcpyHostToDevice, h->stream));
+        SN_CK(h, cudaStreamSynchronize(h->stream));
+        return SN_OK;
+    };
+    sn_status s = SN_OK;
+    if (h->stalled_item >= 0) {  // restore the planned list
+        if ((s = put(h->stalled_item, &h->deps_host[(size_t)(h->flow_off[0] + h->stalled_item) * SN_MAX_DEPS])))
+            return s;
+        h->stalled_item = -1;
+    }
+    if (item < 0) return SN_OK;
+    int dl[SN_MAX_DEPS];
+    memcpy(dl, &h->deps_host[(size_t)(h->flow_off[0] + item) * SN_MAX_DEPS], sizeof(dl));
+    // the spare flag sits past the last work entry; items index done[] from the variant's offset
+    dl[1] = (int)h->done_n - h->flow_off[0];
+    if (dl[0] < 1) dl[0] = 1;
+    if ((s = put(item, dl))) return s;
+    h->stalled_item = item;
+    return SN_OK;
 }
 
 void *sn_gpu_host_alloc(size_t bytes)
@@ -1748,7 +2048,7 @@ sn_status sn_gpu_flow_stats(sn_handle *h, uint64_t *stats)
     uint32_t e[4] = {0, 0, 0, 0};
     if (h->flow && h->d_err) {
         SN_CK(h, cudaMemcpyAsync(e, h->d_err, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
-        SN_CK(h, cudaMemsetAsync(h->d_err + 1, 0, 3 * sizeof(uint32_t), h->stream));
+        SN_CK(h, cudaMemsetAsync(h->d_err + 1, 0, 2 * sizeof(uint32_t), h->stream));
         SN_CK(h, cudaStreamSynchronize(h->stream));
     }
     stats[0] = h->flow ? 1 : 0;

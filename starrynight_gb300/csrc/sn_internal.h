@@ -35,6 +35,7 @@
 #define SN_UPLOAD_FIELD_STREAMS 2
 #endif
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
+#define SN_CACHED_THREADS 256    // block size of the cached-field sweep kernel
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log
 
 // Geometry of one replica's tiles: block dims, tile dims (block + halo),
@@ -60,6 +61,15 @@ struct SnTile {
     int start[3][SN_MAX_S];
     int smem_bytes;  // dynamic shared memory for the sweep kernel
     int field_smem;  // dynamic shared memory for the field kernel
+    // Cached-field sweep (cmode = 1; sn_sweep_cached.cuh).  Its tile is the
+    // block + halo with the z halo rounded up to 4 sites (16-byte rows), one
+    // int32 array per field component, plain slots (ux*cT[1] + uy)*cT[2] + uz.
+    int cmode;
+    int cT[3];       // tile dims
+    int cH[3];       // halo per axis (z: cutoff rounded up to a multiple of 4)
+    int cslots;      // cT[0]*cT[1]*cT[2]
+    int cpc;         // colour groups whose proposals are staged at once
+    int csmem;       // dynamic shared memory of the cached sweep kernel
 };
 
 struct SnReplicaDev {
@@ -76,6 +86,12 @@ struct SnReplicaDev {
     // (mapped pinned host memory or device memory) that receives every
     // block's final sites (x, y, z per site, site order) as the block ends.
     float *out_xyz;
+    // Local-field cache of the cached-field sweep (null: none): 3 int32
+    // arrays of N (x, y, z components), g_i = len_i sum_j len_j T_ij p_j -
+    // CageStrain sum_nn p_j in fixed point, value = int * ginv.
+    int *gcache;
+    float gscale;      // 2^k: float -> fixed point
+    float ginv;        // 2^-k
 };
 
 // Per-replica sweep accumulators (zeroed at the end of every sweep).
@@ -114,18 +130,24 @@ struct SnPhaseArgs {
 };
 
 #define SN_MAX_DEPS 28            // 1 count + up to 26 adjacent blocks (+1 spare)
-#define SN_WAIT_LIMIT (1 << 22)   // polls of a dependency flag before SN_ERR_TIMEOUT
+// Default polls of a dependency flag before a block gives up with
+// SN_ERR_TIMEOUT (about 1-4 s); a handle may lower it (sn_gpu_set_wait_limit).
+#define SN_WAIT_LIMIT_DEFAULT (1u << 22)
 
 // Dataflow sweep: the work list holds every block of a kernel variant in
 // block-colour order; deps[item*SN_MAX_DEPS] = count, then the items of the
 // adjacent blocks with an earlier colour; done[item] = last sweep (epoch)
 // that finished the block; queue = next item to take (reset every sweep).
+// The done array has one spare flag past the last item that no block ever
+// publishes (a test hook points a dependency at it to exercise the timeout).
 struct SnFlowArgs {
     SnPhaseArgs base;
     const int *deps;
     uint32_t *done;
     uint32_t *queue;
-    uint32_t *err;  // [0] wait timed out, [1] items that waited, [2] polls
+    // [0] a wait timed out, [1] items that waited, [2] polls, [3] poll limit
+    // per dependency (set by the host; read by every waiting thread)
+    uint32_t *err;
 };
 
 // Neighbour offset table for the per-site kernels (energy, adjoint, quench).

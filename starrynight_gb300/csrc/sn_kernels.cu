@@ -62,6 +62,8 @@ __global__ void upload_convert_kernel(const float *__restrict__ sxyz, const floa
             x = y = z = 0.0f;
         } else {
             if (!mixed && L != uniform_len) atomicOr(&flags[0], 1);
+            // the field cache's fixed-point range assumes unit (or shorter) dipole components
+            if (!(fabsf(x) <= 1.0001f && fabsf(y) <= 1.0001f && fabsf(z) <= 1.0001f)) atomicOr(&flags[3], 1);
         }
         px[i] = x;
         py[i] = y;
@@ -267,6 +269,23 @@ cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnRe
                                 uint32_t *sweep, SnExchange *ex, int *order, uint32_t *queues, cudaStream_t st)
 {
     sweep_end_kernel<<<1, 256, 0, st>>>(acc, state, hist, reps, nrep, sweep, ex, order, queues);
+    return cudaGetLastError();
+}
+
+__global__ void count_diff_kernel(const int *__restrict__ a, const int *__restrict__ b, long long n,
+                                  unsigned long long *count)
+{
+    unsigned long long c = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        c += a[i] != b[i];
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+cudaError_t sn_launch_count_diff(const int *a, const int *b, long long n, unsigned long long *count, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    count_diff_kernel<<<grid_for(n, 256), 256, 0, st>>>(a, b, n, count);
     return cudaGetLastError();
 }
 

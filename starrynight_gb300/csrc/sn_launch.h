@@ -13,17 +13,22 @@ struct SnFieldArgs;
 
 struct SnFieldArgsHost;
 
-typedef cudaError_t (*sn_sweep_launch_fn)(bool two_d, bool mixed, const SnPhaseArgs &a, int grid, int threads,
-                                          int smem, cudaStream_t st);
+typedef cudaError_t (*sn_sweep_launch_fn)(bool two_d, bool mixed, bool cached, const SnPhaseArgs &a, int grid,
+                                          int threads, int smem, cudaStream_t st);
 typedef cudaError_t (*sn_field_launch_fn)(bool fp64, bool two_d, bool mixed, const void *field_args, int grid,
                                           int threads, int smem, cudaStream_t st);
 typedef void (*sn_geo_fn)(bool two_d, int *S, int *SZ, int *NS, int *NF, int *merge);
-typedef cudaError_t (*sn_flow_launch_fn)(bool two_d, bool mixed, const SnFlowArgs &a, int grid, int threads, int smem,
-                                         cudaStream_t st, int *max_grid);
+typedef cudaError_t (*sn_flow_launch_fn)(bool two_d, bool mixed, bool cached, const SnFlowArgs &a, int grid,
+                                         int threads, int smem, cudaStream_t st, int *max_grid);
+typedef int (*sn_cached_smem_fn)(int cslots, int tg, int pc, bool mixed);
+typedef cudaError_t (*sn_gfield_launch_fn)(bool mixed, const void *field_args, int grid, int smem, cudaStream_t st);
 
 #define SN_DECLARE_RC(N)                                                                                     \
-    cudaError_t sn_launch_sweep_rc##N(bool, bool, const SnPhaseArgs &, int, int, int, cudaStream_t);        \
-    cudaError_t sn_launch_flow_rc##N(bool, bool, const SnFlowArgs &, int, int, int, cudaStream_t, int *);   \
+    cudaError_t sn_launch_sweep_rc##N(bool, bool, bool, const SnPhaseArgs &, int, int, int, cudaStream_t);  \
+    cudaError_t sn_launch_flow_rc##N(bool, bool, bool, const SnFlowArgs &, int, int, int, cudaStream_t,     \
+                                     int *);                                                               \
+    int sn_cached_smem_rc##N(int, int, int, bool);                                                         \
+    cudaError_t sn_launch_gfield_rc##N(bool, const void *, int, int, cudaStream_t);                        \
     cudaError_t sn_launch_field_rc##N(bool, bool, bool, const void *, int, int, int, cudaStream_t);        \
     cudaError_t sn_launch_field64_rc##N(bool, bool, const void *, int, int, int, cudaStream_t);            \
     void sn_geo_rc##N(bool, int *, int *, int *, int *, int *);
@@ -46,6 +51,7 @@ struct SnFieldArgsHost {
     float *grad;
     double *red;
     int red_stride;
+    int write_g;
 };
 
 // Exchange bookkeeping on the device.
@@ -86,6 +92,8 @@ cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnRe
                                 uint32_t *sweep, SnExchange *ex, int *order, uint32_t *queues, cudaStream_t st);
 cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
                                        double cage, double *drift_max, int record, cudaStream_t st);
+// *count += number of i < n with a[i] != b[i].
+cudaError_t sn_launch_count_diff(const int *a, const int *b, long long n, unsigned long long *count, cudaStream_t st);
 cudaError_t sn_launch_quench_step(float *px, float *py, float *pz, const float *len, const float *grad,
                                   long long n, float step, cudaStream_t st);
 cudaError_t sn_launch_fma_peak(float *out, int blocks, int threads, int iters, cudaStream_t st);

@@ -24,7 +24,11 @@
 //
 // The first call on each device looks up the array's device address with
 // cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture begins.
+// first call before any stream capture begins.  The cache is per process:
+// after cudaDeviceReset the module is loaded again and the cached address is
+// stale, so a process that resets a device must not call this entry point on
+// that device afterwards.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 
@@ -49,7 +53,9 @@ static __device__ __align__(256) unsigned char sn_noalloc_scratch[kScratchBytes]
 
 // Device address of sn_noalloc_scratch per device (host-side cache).  In host
 // code the symbol's own name is only a host stand-in, never a device address.
-void *g_scratch[SN_NOALLOC_MAX_DEVICES];
+// Host threads may race on the first call of a device: both look the address
+// up (the same value) and store it atomically.
+std::atomic<void *> g_scratch[SN_NOALLOC_MAX_DEVICES];
 
 thread_local char g_err[256];
 
@@ -86,16 +92,18 @@ sn_status sn_gpu_energy_noalloc(const float *d_px, const float *d_py, const floa
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nfail(SN_ERR_CUDA, "no CUDA device");
     if (dev < 0 || dev >= SN_NOALLOC_MAX_DEVICES) return nfail(SN_ERR_UNSUPPORTED, "device index too large");
-    if (!g_scratch[dev]) {
+    void *cached = g_scratch[dev].load(std::memory_order_acquire);
+    if (!cached) {
         void *ptr = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&ptr, sn_noalloc_scratch);
         if (e != cudaSuccess || !ptr) {
             snprintf(g_err, sizeof(g_err), "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
             return nfail(SN_ERR_CUDA, g_err);
         }
-        g_scratch[dev] = ptr;
+        g_scratch[dev].store(ptr, std::memory_order_release);
+        cached = ptr;
     }
-    unsigned char *base = (unsigned char *)g_scratch[dev];
+    unsigned char *base = (unsigned char *)cached;
 
     SnTile tile;
     char why[200];

@@ -34,6 +34,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "sn_device.cuh"
 
 namespace sn_sweep {
@@ -60,6 +62,10 @@ struct Geo {
 };
 
 __device__ __forceinline__ float sn_fma(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Round to the nearest integer (ties to even), saturating at the int32 range.
+__device__ __forceinline__ int fixed_point(float v) { return __float2int_rn(v); }
+__device__ __forceinline__ int fixed_point(double v) { return __double2int_rn(v); }
 
 // Sum of component c over the accumulator sets, in set order.
 template <typename R>
@@ -508,75 +514,6 @@ __device__ __forceinline__ void sweep_block(const SnWork w, const SnPhaseArgs &a
     }
 }
 
-// One block colour per launch, one CTA per block.
-template <int RC, bool TWO_D, bool MIXED>
-__global__ void __launch_bounds__(SN_SWEEP_MAX_THREADS, SN_SWEEP_MIN_BLOCKS) sweep_phase(const SnPhaseArgs a)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    sweep_block<RC, TWO_D, MIXED, false>(a.work[blockIdx.x], a, smem);
-}
-
-__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p)
-{
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release_gpu(uint32_t *p, uint32_t v)
-{
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// Dataflow sweep: one persistent launch per sweep.  Every CTA is resident
-// (the host sizes the grid with the occupancy API) and takes blocks from a
-// queue ordered by block colour.  Before updating a block it waits until
-// each adjacent block of an earlier colour has finished this sweep (a
-// bounded spin; on time-out it records SN_ERR_TIMEOUT in *err and goes on).
-// Adjacent blocks of later colours wait for this one in turn, so every block
-// sees exactly the lattice the phase-by-phase order gives it.  Deadlock
-// cannot occur: a block waited on was taken from the queue earlier by a CTA
-// that is running, and it only waits on blocks taken before it.
-template <int RC, bool TWO_D, bool MIXED>
-__global__ void __launch_bounds__(SN_SWEEP_MAX_THREADS, SN_SWEEP_MIN_BLOCKS) sweep_flow(const SnFlowArgs f)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_item;
-    const int tid = threadIdx.x;
-    const uint32_t epoch = *f.base.sweep + 1u;
-    for (;;) {
-        if (tid == 0) s_item = (int)atomicAdd(f.queue, 1u);
-        __syncthreads();
-        const int item = s_item;
-        __syncthreads();
-        if (item >= f.base.n_work) break;
-        const int *dl = f.deps + (size_t)item * SN_MAX_DEPS;
-        if (tid < dl[0]) {
-            const uint32_t *flag = f.done + dl[1 + tid];
-            int it = 0;
-            for (; ld_acquire_gpu(flag) < epoch; it++) {
-                if (it >= SN_WAIT_LIMIT) {
-                    atomicOr(f.err, 1u);
-                    break;
-                }
-                __nanosleep(100);
-            }
-            if (it) {  // dependency stall statistics
-                atomicAdd(f.err + 1, 1u);
-                atomicAdd(f.err + 2, (unsigned)it);
-            }
-        }
-        __syncthreads();
-        __threadfence();
-        sweep_block<RC, TWO_D, MIXED, true>(f.base.work[item], f.base, smem);
-        __syncthreads();
-        if (tid == 0) {
-            __threadfence();
-            st_release_gpu(f.done + item, epoch);
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Full local-field pass (energy recompute, site energies, adjoint).  Same
 // tiles, stencil and thread roles as the sweep, read-only, every block of
@@ -596,7 +533,102 @@ struct SnFieldArgs {
     float *grad;     // nullable: 3N floats (interleaved)
     double *red;     // 10 doubles per replica
     int red_stride;  // doubles between replicas in red (0: all replicas share one slot)
+    int write_g;     // 1: refresh the replica's local-field cache (SnReplicaDev::gcache)
 };
+
+}  // namespace sn_sweep
+
+#include "sn_sweep_cached.cuh"
+
+namespace sn_sweep {
+
+// Block size limits of a sweep kernel variant: the stencil-sum sweep (its
+// thread count varies with the block shape) or the cached-field sweep (fixed).
+template <bool CACHED>
+struct SweepBounds {
+    static constexpr int threads = CACHED ? SN_CACHED_THREADS : SN_SWEEP_MAX_THREADS;
+    static constexpr int min_blocks = CACHED ? 2 : SN_SWEEP_MIN_BLOCKS;
+};
+
+template <int RC, bool TWO_D, bool MIXED, bool CACHED, bool FLOW>
+__device__ __forceinline__ void sweep_block_any(const SnWork w, const SnPhaseArgs &a, unsigned char *smem)
+{
+    if constexpr (CACHED && !TWO_D) sweep_block_cached<RC, MIXED, FLOW>(w, a, smem);
+    else sweep_block<RC, TWO_D, MIXED, FLOW>(w, a, smem);
+}
+
+// One block colour per launch, one CTA per block.
+template <int RC, bool TWO_D, bool MIXED, bool CACHED>
+__global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACHED>::min_blocks)
+    sweep_phase(const SnPhaseArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    sweep_block_any<RC, TWO_D, MIXED, CACHED, false>(a.work[blockIdx.x], a, smem);
+}
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(uint32_t *p, uint32_t v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Dataflow sweep: one persistent launch per sweep.  Every CTA is resident
+// (the host sizes the grid with the occupancy API) and takes blocks from a
+// queue ordered by block colour.  Before updating a block it waits until
+// each adjacent block of an earlier colour has finished this sweep (a spin
+// bounded by err[3] polls; on time-out it records SN_ERR_TIMEOUT in err[0]
+// and goes on, so the launch always ends).
+// Adjacent blocks of later colours wait for this one in turn, so every block
+// sees exactly the lattice the phase-by-phase order gives it.  Deadlock
+// cannot occur: a block waited on was taken from the queue earlier by a CTA
+// that is running, and it only waits on blocks taken before it.
+template <int RC, bool TWO_D, bool MIXED, bool CACHED>
+__global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACHED>::min_blocks)
+    sweep_flow(const SnFlowArgs f)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    const uint32_t epoch = *f.base.sweep + 1u;
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(f.queue, 1u);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= f.base.n_work) break;
+        const int *dl = f.deps + (size_t)item * SN_MAX_DEPS;
+        if (tid < dl[0]) {
+            const uint32_t *flag = f.done + dl[1 + tid];
+            const uint32_t limit = __ldcg(f.err + 3);
+            uint32_t it = 0;
+            for (; ld_acquire_gpu(flag) < epoch; it++) {
+                if (it >= limit) {
+                    atomicOr(f.err, 1u);
+                    break;
+                }
+                __nanosleep(100);
+            }
+            if (it) {  // dependency stall statistics
+                atomicAdd(f.err + 1, 1u);
+                atomicAdd(f.err + 2, (unsigned)it);
+            }
+        }
+        __syncthreads();
+        __threadfence();
+        sweep_block_any<RC, TWO_D, MIXED, CACHED, true>(f.base.work[item], f.base, smem);
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            st_release_gpu(f.done + item, epoch);
+        }
+    }
+}
 
 template <typename R, int RC, bool TWO_D, bool MIXED>
 __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldArgs a)
@@ -675,6 +707,15 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
                                (TWO_D ? 0 : w.z0 + cz + S * qz);
         const R px = (R)gpx[site], py = (R)gpy[site], pz = (R)gpz[site];
         const R Li = (R)glen[site];  // 0 at vacancies in both modes
+        if (a.write_g && Rp.gcache) {
+            // the cached-field sweep's g = len_i H_i - C nn_i (no applied field), fixed point
+            const R scl = MIXED ? R(1) : Lu;
+            const R s = (R)Rp.gscale;
+            const size_t Nn = (size_t)Rp.n_sites;
+            Rp.gcache[site] = fixed_point(s * (Li * scl * hx - C * nnv[0]));
+            Rp.gcache[Nn + site] = fixed_point(s * (Li * scl * hy - C * nnv[1]));
+            Rp.gcache[2 * Nn + site] = fixed_point(s * (Li * scl * hz - C * nnv[2]));
+        }
         if (Li == R(0)) {
             if (a.site_e) a.site_e[site] = 0.0;
             if (a.grad) {
@@ -728,63 +769,80 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
     }
 }
 
+// The dynamic shared-memory limit of a kernel is a per-device attribute: it
+// is set once per (kernel variant, device), tracked by one bit per variant in
+// a per-device mask (a second host thread may set it again: harmless).
+#define SN_ATTR_MAX_DEVICES 64
+struct SnAttrOnce {
+    std::atomic<uint32_t> mask[SN_ATTR_MAX_DEVICES];
+};
+
+template <typename F>
+cudaError_t set_smem_once(SnAttrOnce &once, int idx, F fn, int static_bytes)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint32_t bit = 1u << idx;
+    const bool tracked = dev >= 0 && dev < SN_ATTR_MAX_DEVICES;
+    if (tracked && (once.mask[dev].load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    if (static_bytes < 0) {  // static shared memory of the kernel comes off the 227 KB
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, fn);
+        if (e != cudaSuccess) return e;
+        static_bytes = (int)fa.sharedSizeBytes;
+    }
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - static_bytes);
+    if (e == cudaSuccess && tracked) once.mask[dev].fetch_or(bit, std::memory_order_release);
+    return e;
+}
+
 template <typename R, int RC>
 cudaError_t launch_field_rc(bool two_d, bool mixed, const SnFieldArgs &args, int grid, int threads, int smem_bytes,
                             cudaStream_t st)
 {
-    static bool configured[4] = {false, false, false, false};
+    static SnAttrOnce once;
     const int idx = (two_d ? 2 : 0) + (mixed ? 1 : 0);
     void (*fn)(const SnFieldArgs);
     if (two_d) fn = mixed ? field_tiled<R, RC, true, true> : field_tiled<R, RC, true, false>;
     else fn = mixed ? field_tiled<R, RC, false, true> : field_tiled<R, RC, false, false>;
-    if (!configured[idx]) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (e != cudaSuccess) return e;
-        configured[idx] = true;
-    }
+    if (cudaError_t e = set_smem_once(once, idx, fn, 0)) return e;
     if (grid <= 0) return cudaSuccess;
     fn<<<grid, threads, smem_bytes, st>>>(args);
     return cudaGetLastError();
 }
 
+// The cached-field variants exist for 3D lattices only.
 template <int RC>
-cudaError_t launch_rc(bool two_d, bool mixed, const SnPhaseArgs &args, int grid, int threads, int smem_bytes,
-                      cudaStream_t st)
+cudaError_t launch_rc(bool two_d, bool mixed, bool cached, const SnPhaseArgs &args, int grid, int threads,
+                      int smem_bytes, cudaStream_t st)
 {
-    static bool configured[4] = {false, false, false, false};
-    const int idx = (two_d ? 2 : 0) + (mixed ? 1 : 0);
+    static SnAttrOnce once;
+    if (cached && two_d) return cudaErrorNotSupported;
+    const int idx = (cached ? 4 : 0) + (two_d ? 2 : 0) + (mixed ? 1 : 0);
     void (*fn)(const SnPhaseArgs);
-    if (two_d) fn = mixed ? sweep_phase<RC, true, true> : sweep_phase<RC, true, false>;
-    else fn = mixed ? sweep_phase<RC, false, true> : sweep_phase<RC, false, false>;
-    if (!configured[idx]) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (e != cudaSuccess) return e;
-        configured[idx] = true;
-    }
+    if (cached) fn = mixed ? sweep_phase<RC, false, true, true> : sweep_phase<RC, false, false, true>;
+    else if (two_d) fn = mixed ? sweep_phase<RC, true, true, false> : sweep_phase<RC, true, false, false>;
+    else fn = mixed ? sweep_phase<RC, false, true, false> : sweep_phase<RC, false, false, false>;
+    if (cudaError_t e = set_smem_once(once, idx, fn, 0)) return e;
     if (grid <= 0) return cudaSuccess;
     fn<<<grid, threads, smem_bytes, st>>>(args);
     return cudaGetLastError();
 }
 
 template <int RC>
-cudaError_t launch_flow_rc(bool two_d, bool mixed, const SnFlowArgs &args, int grid, int threads, int smem_bytes,
-                           cudaStream_t st, int *max_grid)
+cudaError_t launch_flow_rc(bool two_d, bool mixed, bool cached, const SnFlowArgs &args, int grid, int threads,
+                           int smem_bytes, cudaStream_t st, int *max_grid)
 {
-    static bool configured[4] = {false, false, false, false};
-    const int idx = (two_d ? 2 : 0) + (mixed ? 1 : 0);
+    static SnAttrOnce once;
+    if (cached && two_d) return cudaErrorNotSupported;
+    const int idx = (cached ? 4 : 0) + (two_d ? 2 : 0) + (mixed ? 1 : 0);
     void (*fn)(const SnFlowArgs);
-    if (two_d) fn = mixed ? sweep_flow<RC, true, true> : sweep_flow<RC, true, false>;
-    else fn = mixed ? sweep_flow<RC, false, true> : sweep_flow<RC, false, false>;
-    if (!configured[idx]) {
-        // the queue slot is static shared memory: the dynamic limit is what remains of 227 KB
-        cudaFuncAttributes fa;
-        cudaError_t e = cudaFuncGetAttributes(&fa, fn);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     227 * 1024 - (int)fa.sharedSizeBytes);
-        if (e != cudaSuccess) return e;
-        configured[idx] = true;
-    }
+    if (cached) fn = mixed ? sweep_flow<RC, false, true, true> : sweep_flow<RC, false, false, true>;
+    else if (two_d) fn = mixed ? sweep_flow<RC, true, true, false> : sweep_flow<RC, true, false, false>;
+    else fn = mixed ? sweep_flow<RC, false, true, false> : sweep_flow<RC, false, false, false>;
+    // the queue slot is static shared memory: the dynamic limit is what remains of 227 KB
+    if (cudaError_t e = set_smem_once(once, idx, fn, -1)) return e;
     if (max_grid) {
         int per_sm = 0, dev = 0, nsm = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem_bytes);
@@ -795,6 +853,17 @@ cudaError_t launch_flow_rc(bool two_d, bool mixed, const SnFlowArgs &args, int g
     }
     if (grid <= 0) return cudaSuccess;
     fn<<<grid, threads, smem_bytes, st>>>(args);
+    return cudaGetLastError();
+}
+
+template <int RC>
+cudaError_t launch_gfield_rc(bool mixed, const SnFieldArgs &args, int grid, int smem_bytes, cudaStream_t st)
+{
+    static SnAttrOnce once;
+    void (*fn)(const SnFieldArgs) = mixed ? gfield_tiled<RC, true> : gfield_tiled<RC, false>;
+    if (cudaError_t e = set_smem_once(once, mixed ? 1 : 0, fn, 0)) return e;
+    if (grid <= 0) return cudaSuccess;
+    fn<<<grid, SN_CACHED_THREADS, smem_bytes, st>>>(args);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,586 @@
+// sn_sweep_cached.cuh -- the cached-field Metropolis sweep of one block.
+//
+// The energy change of a move at site i is dE = (p' - p).(g_i + E) (+ the K
+// term) with the local field g_i = len_i sum_j len_j T_ij p_j - CageStrain
+// sum_nn p_j (src/starrynight-montecarlo-core.c:91-134: site_energy's
+// dipole, cage-strain and field terms).  g is linear in the neighbours'
+// dipoles, so instead of summing the cutoff stencil for every attempted move
+// (what sweep_block does), this kernel keeps g of every site in HBM and, when
+// a move at site a is accepted, adds the change of every neighbour's field,
+// dg_{a+o} = len_{a+o} len_a T_o dp_a - CageStrain [|o| = 1] dp_a, for the
+// offsets o of the cutoff sphere.  An attempt then costs one read of g_i; the
+// stencil work is spent only on accepted moves.  The result of every move is
+// that of the stencil sum up to rounding (the field is the same linear sum).
+//
+// Fixed point, exactly.  Each neighbour's contribution is rounded to a
+// fixed-point grid of 2^-k on its own, Q(c_ij) with c_ij = w (T_o p_j) -
+// CageStrain [|o| = 1] p_j, w = len_i len_j, and g_i is the int32 sum of
+// those integers.  A move of site a from p to p' then changes g_n by exactly
+// Q(c(p')) - Q(c(p)), which the sweep adds with integer atomics: integer
+// addition is associative, so g after any sequence of moves equals, bit for
+// bit, the g that the field pass (gfield_tiled) computes from scratch for
+// the current lattice -- independent of thread order, schedule, batching or
+// a resume from a checkpoint, and free of drift.  k is chosen on the host so
+// that |c * 2^k| < 2^22 for every contribution; Q is then one FMA with a
+// magic constant (round to nearest even), the same operation everywhere.
+//
+// Ownership.  A block's tile is the block plus a halo of `cutoff` sites
+// (the z halo rounded up to 4 sites for 16-byte rows).  It is loaded when the
+// block starts and the WHOLE tile is stored back when the block ends: with
+// every block side >= 2 cutoff (a planner condition), tiles of blocks that
+// can run at the same time (not adjacent) are disjoint, and adjacent blocks
+// run one after the other (block colours; the dataflow kernel's dependency
+// waits), so each site's g is held by at most one running block.
+#pragma once
+
+namespace sn_sweep {
+
+// Shared-memory carve-up of the cached sweep, identical on host and device.
+struct CCarve {
+    uint32_t tile, tlen, props, list, pairs, cnt, red, total;
+};
+
+__host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, bool mixed)
+{
+    CCarve c;
+    uint32_t o = 0;
+    c.tile = o;
+    o += sn_align16(3u * (uint32_t)cslots * 4u);
+    c.tlen = o;
+    if (mixed) o += sn_align16((uint32_t)cslots * 4u);
+    c.props = o;
+    o += (uint32_t)(pc * tg) * 32u;  // (p', threshold), (p_old, -) per target
+    c.list = o;
+    o += (uint32_t)tg * 32u;         // accepted moves of a group
+    c.pairs = o;
+    o += sn_align16((uint32_t)np * 48u);
+    c.cnt = o;
+    o += 16u;
+    c.red = o;
+    o += (SN_CACHED_THREADS / 32) * 16u * 8u;
+    c.total = o;
+    return c;
+}
+
+// One stencil pair's constants in shared memory: T_o (xx yy zz xy xz yz),
+// the offset, and whether |o| = 1 (cage strain).
+struct CPair {
+    float t[6];
+    int o[3];
+    int nn;
+    int pad[2];
+};
+static_assert(sizeof(CPair) == 48, "pair record");
+
+// Q(v * 2^k) for |v * 2^k| < 2^22: adding 1.5 * 2^23 leaves round-to-nearest-
+// even(v * 2^k) in the low mantissa bits (the scaling by a power of two is exact).
+#define SN_Q_MAGIC 12582912.0f  // 1.5 * 2^23
+#define SN_Q_MAGIC_BITS 0x4B400000u
+__device__ __forceinline__ uint32_t q_bits(float v, float scale) { return __float_as_uint(fmaf(v, scale, SN_Q_MAGIC)); }
+
+// The contribution c = w (T p) - C [nn] p of one dipole p through offset tensor
+// t (xx yy zz xy xz yz), as the raw magic-biased bits of Q(c) per component.
+// Every kernel that builds or updates the field cache calls this function, so
+// the rounding is the same everywhere.
+__device__ __forceinline__ void q_contrib(const float (&t)[6], bool NN, float w, float C, float scale, float px,
+                                          float py, float pz, uint32_t &qx, uint32_t &qy, uint32_t &qz)
+{
+    float vx = fmaf(t[0], px, fmaf(t[3], py, __fmul_rn(t[4], pz)));
+    float vy = fmaf(t[3], px, fmaf(t[1], py, __fmul_rn(t[5], pz)));
+    float vz = fmaf(t[4], px, fmaf(t[5], py, __fmul_rn(t[2], pz)));
+    vx = __fmul_rn(w, vx);
+    vy = __fmul_rn(w, vy);
+    vz = __fmul_rn(w, vz);
+    if (NN) {
+        vx = __fsub_rn(vx, __fmul_rn(C, px));
+        vy = __fsub_rn(vy, __fmul_rn(C, py));
+        vz = __fsub_rn(vz, __fmul_rn(C, pz));
+    }
+    qx = q_bits(vx, scale);
+    qy = q_bits(vy, scale);
+    qz = q_bits(vz, scale);
+}
+
+template <int RC, int I>
+__device__ __forceinline__ void put_pair(CPair *tab)
+{
+    constexpr sn_stencil::Off o = sn_stencil::pair_offset(RC, false, I);
+    CPair p;
+#pragma unroll
+    for (int e = 0; e < 6; e++) p.t[e] = 0.0f;
+    p.t[0] = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 0);
+    p.t[1] = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 1);
+    p.t[2] = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 2);
+    p.t[3] = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 3);
+    p.t[4] = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 4);
+    p.t[5] = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 5);
+    p.o[0] = o.x;
+    p.o[1] = o.y;
+    p.o[2] = o.z;
+    p.nn = (o.x * o.x + o.y * o.y + o.z * o.z == 1) ? 1 : 0;
+    p.pad[0] = p.pad[1] = 0;
+    tab[I] = p;
+}
+
+// Thread k of the CTA writes pairs k, k + nthreads, ... of the table.
+template <int RC, int... Is>
+__device__ __forceinline__ void fill_pairs(std::integer_sequence<int, Is...>, CPair *tab, int tid, int nthreads)
+{
+    ((tid == Is % nthreads ? put_pair<RC, Is>(tab) : void()), ...);
+}
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+
+// Copy (store = false) or write back (store = true) the tile of block w:
+// cT[0] x cT[1] rows of cT[2] consecutive z sites per array, in 16-byte
+// chunks.  Z, the block origin and the z halo are multiples of 4, so a chunk
+// never straddles the periodic wrap.
+template <bool STORE>
+__device__ __forceinline__ void move_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, int *tile,
+                                          float *tlen, int tid, int nthreads)
+{
+    const int X = R.X, Y = R.Y, Z = R.Z;
+    const int T1 = Gm.cT[1], T2 = Gm.cT[2], cpr = T2 >> 2;
+    const int rows = Gm.cT[0] * T1;
+    const long long N = R.n_sites;
+    const int cs = Gm.cslots;
+    const int narr = tlen ? 4 : 3;
+    const int total = rows * cpr;
+    for (int idx = tid; idx < total * narr; idx += nthreads) {
+        const int arr = idx / total, rem = idx - arr * total;
+        const int row = rem / cpr, c = rem - row * cpr;
+        const int ux = row / T1, uy = row - ux * T1;
+        const int gx = sn_wrap(w.x0 - Gm.cH[0] + ux, X), gy = sn_wrap(w.y0 - Gm.cH[1] + uy, Y);
+        const int gz = sn_wrap(w.z0 - Gm.cH[2] + 4 * c, Z);
+        const long long g = ((long long)gx * Y + gy) * Z + gz;
+        const int slot = row * T2 + 4 * c;
+        if (arr < 3) {
+            int *src = R.gcache + arr * N + g;
+            int *dst = tile + arr * cs + slot;
+            if (STORE) {
+                *reinterpret_cast<int4 *>(src) = *reinterpret_cast<const int4 *>(dst);
+            } else {
+                cp_async16(dst, src);
+            }
+        } else if (!STORE) {
+            cp_async16(tlen + slot, R.len + g);
+        }
+    }
+}
+
+template <int RC, bool MIXED, bool FLOW>
+__device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhaseArgs &a, unsigned char *smem)
+{
+    using G = Geo<RC, false>;
+    constexpr int S = G::S, NP = G::NP;
+    constexpr bool MERGE = G::MERGE;
+    constexpr int NT = SN_CACHED_THREADS;
+    constexpr int PPT = (NP + NT - 1) / NT;     // stencil pairs per thread in the scatter
+    constexpr int GRP = NP >= NT ? 1 : NT / NP;  // accepted moves scattered at once
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const SnReplicaDev &R = a.reps[w.rep];
+    const SnTile &Gm = a.geoms[R.geom];
+    const int Y = R.Y, Z = R.Z;
+    float *__restrict__ gpx = R.px;
+    float *__restrict__ gpy = R.py;
+    float *__restrict__ gpz = R.pz;
+    const float *__restrict__ glen = R.len;
+    const int Bx = Gm.B[0], By = Gm.B[1], Bz = Gm.B[2];
+    const int T1 = Gm.cT[1], T2 = Gm.cT[2];
+    const int tp = Gm.tp, tg = Gm.tg, ng = Gm.ng, pc = Gm.cpc;
+    const int nqy = Gm.nq[1], nqz = Gm.nq[2];
+    const uint32_t sweep = *a.sweep;
+    const uint2 key = make_uint2(R.seed_lo, R.seed_hi);
+    const float beta = R.beta;
+    const float Ex = R.E[0], Ey = R.E[1], Ez = R.E[2];
+    const float C = a.cage, Kk = a.K;
+    const float Lu = R.length;
+    const float gscale = R.gscale, ginv = R.ginv;  // 2^k, 2^-k
+    const int cs = Gm.cslots;
+
+    const CCarve cv = sn_ccarve(cs, tg, pc, NP, MIXED);
+    int *tile = reinterpret_cast<int *>(smem + cv.tile);
+    float *tlen = MIXED ? reinterpret_cast<float *>(smem + cv.tlen) : nullptr;
+    float4 *props = reinterpret_cast<float4 *>(smem + cv.props);
+    float4 *list = reinterpret_cast<float4 *>(smem + cv.list);
+    const CPair *pairs = reinterpret_cast<const CPair *>(smem + cv.pairs);
+    int *cnt = reinterpret_cast<int *>(smem + cv.cnt);
+    double *red = reinterpret_cast<double *>(smem + cv.red);
+
+    move_tile<false>(R, Gm, w, tile, tlen, tid, NT);
+    if (tid < 2) cnt[tid] = 0;
+
+    // this thread's target role (phase A): target tt of every colour group
+    const int tt = tid;
+    const int hh = tt / tp, t = tt - (tt / tp) * tp;
+    const int qz = t % nqz, qy = (t / nqz) % nqy, qx = t / (nqz * nqy);
+    const bool tvalid = tid < tg && qx < Gm.nq[0];
+    const int trel = (S * qx * T1 + S * qy) * T2 + S * qz;
+    const int srel = ((S * qx) * Y + S * qy) * Z + S * qz;
+
+    // this thread's scatter role (phase B): stencil pairs q = pq + k * NT of
+    // the accepted moves e = pj, pj + GRP, ...; the pair's tensor T_o, whether
+    // |o| = 1, and the slot delta of +o in this tile
+    const int pj = NP >= NT ? 0 : tid / NP;
+    const int pq = NP >= NT ? tid : tid - pj * NP;
+    const bool prole = NP >= NT ? true : pj < GRP;
+    const float L2 = __fmul_rn(Lu, Lu);
+    float Tq[PPT][6];
+    int dq[PPT];
+    bool nnp[PPT], qok[PPT];
+
+    KahanF sdE, sPx, sPy, sPz;
+    unsigned int sacc = 0, satt = 0;
+
+    int gchunk = 0, gnext = 0;
+    unsigned long long amask = 0ull;
+    for (int g = 0; g < ng && g < 64; g++) {
+        int cx, cy, cz;
+        group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
+        if (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) && qz < sn_count(Bz, cz, S))
+            amask |= 1ull << g;
+    }
+    for (int g = 0; g < ng; g++) {
+        // ---- proposals, thresholds and old dipoles of the next pc groups ----------
+        if (g == gnext) {
+            __syncthreads();  // previous chunk fully consumed
+            gchunk = g;
+            gnext = min(g + pc, ng);
+            if (tid < tg) {
+                for (int k = 0; k < gnext - g; k++) {
+                    int cx, cy, cz;
+                    group_colour<S, S, MERGE>(g + k, hh, cx, cy, cz);
+                    float4 pr = make_float4(0.0f, 0.0f, 0.0f, -2.0f);  // no target here
+                    float4 po = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if ((g + k < 64) ? ((amask >> (g + k)) & 1ull)
+                                     : (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
+                                        qz < sn_count(Bz, cz, S))) {
+                        const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
+                        pr.w = -1.0f;  // vacancy
+                        if ((FLOW ? __ldcg(glen + site) : glen[site]) != 0.0f) {
+                            po = make_float4(FLOW ? __ldcg(gpx + site) : gpx[site],
+                                             FLOW ? __ldcg(gpy + site) : gpy[site],
+                                             FLOW ? __ldcg(gpz + site) : gpz[site], 0.0f);
+                            float3 p;
+                            float u;
+                            if (!sn_proposal((uint32_t)site, sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
+                                p = make_float3(po.x, po.y, po.z);
+                            // accept iff dE < -ln(u)/beta  <=>  dE < 0 || exp(-beta dE) > u
+                            const float thr = u > 0.0f ? -logf(u) / beta : INFINITY;
+                            pr = make_float4(p.x, p.y, p.z, thr);
+                        }
+                    }
+                    props[2 * (k * tg + tt)] = pr;
+                    props[2 * (k * tg + tt) + 1] = po;
+                }
+            }
+            if (g == 0) {
+                // the pair table, then this thread's pairs (after the barrier below)
+                fill_pairs<RC>(std::make_integer_sequence<int, NP>{}, reinterpret_cast<CPair *>(smem + cv.pairs),
+                               tid, NT);
+                cp_async_wait_all();
+                __syncthreads();
+#pragma unroll
+                for (int k = 0; k < PPT; k++) {
+                    const int q = pq + k * NT;
+                    qok[k] = prole && q < NP;
+                    const CPair &P = pairs[qok[k] ? q : 0];
+                    dq[k] = (P.o[0] * T1 + P.o[1]) * T2 + P.o[2];
+                    nnp[k] = P.nn != 0;
+#pragma unroll
+                    for (int e = 0; e < 6; e++) Tq[k][e] = P.t[e];
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- A. targets of the group: dE from the cached field, accept, record ---------
+        bool acc = false;
+        float dx = 0.0f, dy = 0.0f, dz = 0.0f, Li = Lu;
+        int tslot = 0;
+        if (tid < tg) {
+            int cx, cy, cz;
+            group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
+            const float4 pr = props[2 * ((g - gchunk) * tg + tt)];
+            if (pr.w >= 0.0f) {
+                const float4 po = props[2 * ((g - gchunk) * tg + tt) + 1];
+                tslot = ((cx + Gm.cH[0]) * T1 + (cy + Gm.cH[1])) * T2 + cz + Gm.cH[2] + trel;
+                const float gx = fmaf((float)tile[tslot], ginv, Ex);
+                const float gy = fmaf((float)tile[cs + tslot], ginv, Ey);
+                const float gz = fmaf((float)tile[2 * cs + tslot], ginv, Ez);
+                dx = pr.x - po.x;
+                dy = pr.y - po.y;
+                dz = pr.z - po.z;
+                float dE = fmaf(dx, gx, fmaf(dy, gy, dz * gz));
+                if (Kk > 0.0f) dE -= Kk * ((fabsf(pr.x) - fabsf(po.x)) + (fabsf(pr.y) - fabsf(po.y)));
+                satt++;
+                if (dE < pr.w) {
+                    acc = true;
+                    const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
+                    gpx[site] = pr.x;
+                    gpy[site] = pr.y;
+                    gpz[site] = pr.z;
+                    if (MIXED) Li = tlen[tslot];
+                    sacc++;
+                    sdE.add(dE);
+                    sPx.add(Li * dx);
+                    sPy.add(Li * dy);
+                    sPz.add(Li * dz);
+                }
+            }
+            // accepted moves of the warp go to the group's list at a base taken atomically
+            // (the list order does not matter: the scatter adds integers)
+            const unsigned m = __ballot_sync(0xffffffffu, acc);
+            int base = 0;
+            if (lane == 0 && m) base = atomicAdd(&cnt[g & 1], __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (acc) {
+                const int e = base + __popc(m & ((1u << lane) - 1u));
+                const float4 pr = props[2 * ((g - gchunk) * tg + tt)];
+                const float4 po = props[2 * ((g - gchunk) * tg + tt) + 1];
+                list[2 * e] = make_float4(__int_as_float(tslot), pr.x, pr.y, pr.z);
+                list[2 * e + 1] = make_float4(po.x, po.y, po.z, Li);
+            }
+        }
+        if (tid == NT - 1) cnt[(g + 1) & 1] = 0;  // the next group's counter (last read a group ago)
+        __syncthreads();
+
+        // ---- B. scatter the accepted moves' field changes into the tile --------------
+        // dg_n = Q(c(p')) - Q(c(p)) for n = a +- o (the magic bias cancels)
+        const int n = cnt[g & 1];
+        for (int e = pj; e < n && prole; e += GRP) {
+            const float4 en = list[2 * e], eo = list[2 * e + 1];
+            const int sa = __float_as_int(en.x);
+#pragma unroll
+            for (int k = 0; k < PPT; k++) {
+                if (!qok[k]) continue;
+                const int sp = sa + dq[k], sm = sa - dq[k];
+                uint32_t nx, ny, nz, ox, oy, oz;
+                if constexpr (MIXED) {
+                    const float wp = __fmul_rn(tlen[sp], eo.w), wm = __fmul_rn(tlen[sm], eo.w);
+                    q_contrib(Tq[k], nnp[k], wp, C, gscale, en.y, en.z, en.w, nx, ny, nz);
+                    q_contrib(Tq[k], nnp[k], wp, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
+                    atomicAdd(tile + sp, (int)(nx - ox));
+                    atomicAdd(tile + cs + sp, (int)(ny - oy));
+                    atomicAdd(tile + 2 * cs + sp, (int)(nz - oz));
+                    q_contrib(Tq[k], nnp[k], wm, C, gscale, en.y, en.z, en.w, nx, ny, nz);
+                    q_contrib(Tq[k], nnp[k], wm, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
+                    atomicAdd(tile + sm, (int)(nx - ox));
+                    atomicAdd(tile + cs + sm, (int)(ny - oy));
+                    atomicAdd(tile + 2 * cs + sm, (int)(nz - oz));
+                } else {
+                    q_contrib(Tq[k], nnp[k], L2, C, gscale, en.y, en.z, en.w, nx, ny, nz);
+                    q_contrib(Tq[k], nnp[k], L2, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
+                    const int ix = (int)(nx - ox), iy = (int)(ny - oy), iz = (int)(nz - oz);
+                    atomicAdd(tile + sp, ix);
+                    atomicAdd(tile + cs + sp, iy);
+                    atomicAdd(tile + 2 * cs + sp, iz);
+                    atomicAdd(tile + sm, ix);
+                    atomicAdd(tile + cs + sm, iy);
+                    atomicAdd(tile + 2 * cs + sm, iz);
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- the tile's fields back to HBM ---------------------------------------------
+    move_tile<true>(R, Gm, w, tile, nullptr, tid, NT);
+
+    // ---- the block's final sites to the caller's buffer ---------------------------
+    if (float *out = R.out_xyz) {
+        for (int row = warp; row < Bx * By; row += NT >> 5) {
+            const int lx = row / By, ly = row - (row / By) * By;
+            const long long s0 = (((long long)(w.x0 + lx)) * Y + (w.y0 + ly)) * Z + w.z0;
+            for (int e = lane; e < Bz; e += 32) {
+                out[3 * (s0 + e) + 0] = __ldcg(gpx + s0 + e);
+                out[3 * (s0 + e) + 1] = __ldcg(gpy + s0 + e);
+                out[3 * (s0 + e) + 2] = __ldcg(gpz + s0 + e);
+            }
+        }
+    }
+
+    // ---- block reduction of the move statistics ---------------------------------
+    double v[6] = {sdE.value(), sPx.value(), sPy.value(), sPz.value(), (double)sacc, (double)satt};
+#pragma unroll
+    for (int k = 0; k < 6; k++) v[k] = warp_sum(v[k]);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) red[warp * 16 + k] = v[k];
+    }
+    __syncthreads();
+    if (tid < 6) {
+        double s = 0.0;
+        for (int q = 0; q < (NT >> 5); q++) s += red[q * 16 + tid];
+        SnAccum *A = a.acc + w.rep;
+        if (tid == 0) atomicAdd(&A->dE, s);
+        else if (tid < 4) atomicAdd(&A->dP[tid - 1], s);
+        else if (tid == 4) atomicAdd(&A->acc, (unsigned long long)s);
+        else atomicAdd(&A->att, (unsigned long long)s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Field pass of the cache: g_i = sum_o Q(c(i, i+o)) for every site of a block
+// from a tile of the dipoles (same tile geometry as the cached sweep), plus
+// the replica's energy sums from it.  Each of the 2 NP contributions of a
+// site is rounded on its own (q_contrib), so the result is the sweep's
+// incremental cache bit for bit.  red[rep*stride + k] as SnFieldArgs, except
+// red[0] = 1/2 sum p_i.g_i (dipole + cage-strain energy) and red[1] = 0.
+
+// Rows of block w's tile of float arrays (px, py, pz and, when MIXED, len)
+// into shared memory by 16-byte asynchronous copies.
+template <bool MIXED>
+__device__ __forceinline__ void stage_p_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, float *tp,
+                                             int tid, int nthreads)
+{
+    const int X = R.X, Y = R.Y, Z = R.Z;
+    const int T1 = Gm.cT[1], T2 = Gm.cT[2], cpr = T2 >> 2;
+    const int total = Gm.cT[0] * T1 * cpr;
+    const int cs = Gm.cslots;
+    const float *src[4] = {R.px, R.py, R.pz, R.len};
+    for (int idx = tid; idx < total * (MIXED ? 4 : 3); idx += nthreads) {
+        const int arr = idx / total, rem = idx - arr * total;
+        const int row = rem / cpr, c = rem - row * cpr;
+        const int ux = row / T1, uy = row - ux * T1;
+        const int gx = sn_wrap(w.x0 - Gm.cH[0] + ux, X), gy = sn_wrap(w.y0 - Gm.cH[1] + uy, Y);
+        const int gz = sn_wrap(w.z0 - Gm.cH[2] + 4 * c, Z);
+        cp_async16(tp + arr * cs + row * T2 + 4 * c, src[arr] + (((long long)gx * Y + gy) * Z + gz));
+    }
+}
+
+// Both contributions of stencil pair I to the field of the site in slot `slot`.
+// Zero tensor entries are skipped: that changes at most the sign of a zero,
+// which Q does not see, so the result equals q_contrib's.
+template <int RC, bool MIXED, int I>
+__device__ __forceinline__ void q_pair(const float *__restrict__ tp, int cs, int slot, int T1, int T2, float w_u,
+                                       float Li, float C, float scale, uint32_t &ax, uint32_t &ay, uint32_t &az)
+{
+    constexpr sn_stencil::Off o = sn_stencil::pair_offset(RC, false, I);
+    constexpr float t0 = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 0);
+    constexpr float t1 = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 1);
+    constexpr float t2 = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 2);
+    constexpr float t3 = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 3);
+    constexpr float t4 = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 4);
+    constexpr float t5 = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 5);
+    constexpr bool NN = o.x * o.x + o.y * o.y + o.z * o.z == 1;
+    const int d = (o.x * T1 + o.y) * T2 + o.z;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        const int sj = side ? slot - d : slot + d;
+        const float px = tp[sj], py = tp[cs + sj], pz = tp[2 * cs + sj];
+        const float w = MIXED ? __fmul_rn(Li, tp[3 * cs + sj]) : w_u;
+        // vx = fmaf(t0, px, fmaf(t3, py, t4 * pz)) and so on, without the zero terms
+        float vx = t4 != 0.0f ? __fmul_rn(t4, pz) : 0.0f;
+        if (t3 != 0.0f) vx = fmaf(t3, py, vx);
+        vx = fmaf(t0, px, vx);
+        float vy = t5 != 0.0f ? __fmul_rn(t5, pz) : 0.0f;
+        vy = fmaf(t1, py, vy);
+        if (t3 != 0.0f) vy = fmaf(t3, px, vy);
+        float vz = __fmul_rn(t2, pz);
+        if (t5 != 0.0f) vz = fmaf(t5, py, vz);
+        if (t4 != 0.0f) vz = fmaf(t4, px, vz);
+        if (MIXED || w != 1.0f) {
+            vx = __fmul_rn(w, vx);
+            vy = __fmul_rn(w, vy);
+            vz = __fmul_rn(w, vz);
+        }
+        if (NN) {
+            vx = __fsub_rn(vx, __fmul_rn(C, px));
+            vy = __fsub_rn(vy, __fmul_rn(C, py));
+            vz = __fsub_rn(vz, __fmul_rn(C, pz));
+        }
+        ax += q_bits(vx, scale);
+        ay += q_bits(vy, scale);
+        az += q_bits(vz, scale);
+    }
+}
+
+template <int RC, bool MIXED, int... Is>
+__device__ __forceinline__ void q_pairs(std::integer_sequence<int, Is...>, const float *tp, int cs, int slot, int T1,
+                                        int T2, float w_u, float Li, float C, float scale, uint32_t &ax, uint32_t &ay,
+                                        uint32_t &az)
+{
+    (q_pair<RC, MIXED, Is>(tp, cs, slot, T1, T2, w_u, Li, C, scale, ax, ay, az), ...);
+}
+
+template <int RC, bool MIXED>
+__global__ void __launch_bounds__(SN_CACHED_THREADS, 2) gfield_tiled(const SnFieldArgs a)
+{
+    using G = Geo<RC, false>;
+    constexpr int NP = G::NP, NT = SN_CACHED_THREADS;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const SnWork w = a.work[blockIdx.x];
+    const SnReplicaDev &R = a.reps[w.rep];
+    const SnTile &Gm = a.geoms[R.geom];
+    const int Y = R.Y, Z = R.Z;
+    const int Bx = Gm.B[0], By = Gm.B[1], Bz = Gm.B[2];
+    const int T1 = Gm.cT[1], T2 = Gm.cT[2], cs = Gm.cslots;
+    const float C = (float)a.cage, Kk = (float)a.K;
+    const float Ex = R.E[0], Ey = R.E[1], Ez = R.E[2];
+    const float w_u = __fmul_rn(R.length, R.length);
+    const float scale = R.gscale;
+    const double ginv = (double)R.ginv;
+    const long long N = R.n_sites;
+    float *tp = reinterpret_cast<float *>(smem);
+    double *red = reinterpret_cast<double *>(smem + sn_align16((MIXED ? 4u : 3u) * (uint32_t)cs * 4u));
+
+    stage_p_tile<MIXED>(R, Gm, w, tp, tid, NT);
+    cp_async_wait_all();
+    __syncthreads();
+
+    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int nsite = Bx * By * Bz;
+    for (int i = tid; i < nsite; i += NT) {
+        const int lz = i % Bz, ly = (i / Bz) % By, lx = i / (Bz * By);
+        const int slot = ((lx + Gm.cH[0]) * T1 + ly + Gm.cH[1]) * T2 + lz + Gm.cH[2];
+        const float Lt = MIXED ? tp[3 * cs + slot] : 0.0f;
+        uint32_t ax = 0u, ay = 0u, az = 0u;
+        q_pairs<RC, MIXED>(std::make_integer_sequence<int, NP>{}, tp, cs, slot, T1, T2, w_u, Lt, C, scale, ax, ay, az);
+        const uint32_t bias = (uint32_t)(2 * NP) * SN_Q_MAGIC_BITS;
+        const int gx = (int)(ax - bias), gy = (int)(ay - bias), gz = (int)(az - bias);
+        const long long site = ((long long)(w.x0 + lx) * Y + (w.y0 + ly)) * Z + w.z0 + lz;
+        if (a.write_g) {
+            R.gcache[site] = gx;
+            R.gcache[N + site] = gy;
+            R.gcache[2 * N + site] = gz;
+        }
+        const float px = tp[slot], py = tp[cs + slot], pz = tp[2 * cs + slot];
+        const float Li = R.len[site];  // 0 at vacancies, whose dipole is zero
+        acc[0] += 0.5 * ginv * ((double)px * gx + (double)py * gy + (double)pz * gz);
+        acc[2] += (double)px * Ex + (double)py * Ey + (double)pz * Ez;
+        if (Kk > 0.0f && Li != 0.0f) acc[3] -= (double)Kk * (fabs((double)px) + fabs((double)py));
+        acc[4] += (double)Li * px;
+        acc[5] += (double)Li * py;
+        acc[6] += (double)Li * pz;
+        acc[7] += px;
+        acc[8] += py;
+        acc[9] += pz;
+    }
+#pragma unroll
+    for (int k = 0; k < 10; k++) acc[k] = warp_sum(acc[k]);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) red[warp * 16 + k] = acc[k];
+    }
+    __syncthreads();
+    if (tid < 10 && a.red) {
+        double s = 0.0;
+        for (int q = 0; q < (NT >> 5); q++) s += red[q * 16 + tid];
+        atomicAdd(&a.red[a.red_stride * w.rep + tid], s);
+    }
+}
+
+__host__ __device__ inline int sn_gfield_smem(int cslots, bool mixed)
+{
+    return (int)(sn_align16((mixed ? 4u : 3u) * (uint32_t)cslots * 4u) + (SN_CACHED_THREADS / 32) * 16u * 8u);
+}
+
+}  // namespace sn_sweep

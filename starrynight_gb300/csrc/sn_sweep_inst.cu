@@ -19,16 +19,21 @@
 static_assert(sizeof(SnFieldArgsHost) >= sizeof(sn_sweep::SnFieldArgs), "field args layout");
 
 #if SN_PART == 0 || SN_PART == 1
-cudaError_t SN_CAT(sn_launch_sweep_rc, SN_RC)(bool two_d, bool mixed, const SnPhaseArgs &a, int grid, int threads,
-                                              int smem, cudaStream_t st)
+cudaError_t SN_CAT(sn_launch_sweep_rc, SN_RC)(bool two_d, bool mixed, bool cached, const SnPhaseArgs &a, int grid,
+                                              int threads, int smem, cudaStream_t st)
 {
-    return sn_sweep::launch_rc<SN_RC>(two_d, mixed, a, grid, threads, smem, st);
+    return sn_sweep::launch_rc<SN_RC>(two_d, mixed, cached, a, grid, threads, smem, st);
 }
 
-cudaError_t SN_CAT(sn_launch_flow_rc, SN_RC)(bool two_d, bool mixed, const SnFlowArgs &a, int grid, int threads,
-                                             int smem, cudaStream_t st, int *max_grid)
+cudaError_t SN_CAT(sn_launch_flow_rc, SN_RC)(bool two_d, bool mixed, bool cached, const SnFlowArgs &a, int grid,
+                                             int threads, int smem, cudaStream_t st, int *max_grid)
 {
-    return sn_sweep::launch_flow_rc<SN_RC>(two_d, mixed, a, grid, threads, smem, st, max_grid);
+    return sn_sweep::launch_flow_rc<SN_RC>(two_d, mixed, cached, a, grid, threads, smem, st, max_grid);
+}
+
+int SN_CAT(sn_cached_smem_rc, SN_RC)(int cslots, int tg, int pc, bool mixed)
+{
+    return (int)sn_sweep::sn_ccarve(cslots, tg, pc, sn_sweep::Geo<SN_RC, false>::NP, mixed).total;
 }
 
 void SN_CAT(sn_geo_rc, SN_RC)(bool two_d, int *S, int *SZ, int *NS, int *NF, int *merge)
@@ -47,6 +52,13 @@ cudaError_t SN_CAT(sn_launch_field64_rc, SN_RC)(bool two_d, bool mixed, const vo
 #endif
 
 #if SN_PART == 0 || SN_PART == 2
+cudaError_t SN_CAT(sn_launch_gfield_rc, SN_RC)(bool mixed, const void *field_args, int grid, int smem,
+                                               cudaStream_t st)
+{
+    const sn_sweep::SnFieldArgs &fa = *static_cast<const sn_sweep::SnFieldArgs *>(field_args);
+    return sn_sweep::launch_gfield_rc<SN_RC>(mixed, fa, grid, smem, st);
+}
+
 cudaError_t SN_CAT(sn_launch_field_rc, SN_RC)(bool fp64, bool two_d, bool mixed, const void *field_args, int grid,
                                               int threads, int smem, cudaStream_t st)
 {

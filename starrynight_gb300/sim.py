@@ -37,6 +37,9 @@ class ModelParams:
     constrain_to_x: bool = False      # ConstrainToX
     dim: int = 3
     seed: int = 1
+    # "auto", "stencil" (sum the cutoff stencil per move) or "cached"
+    # (incremental local fields); see SN_SWEEP_* in include/sn_gpu.h
+    sweep_method: str = "auto"
 
     def to_c(self) -> _abi.Params:
         if len(self.dipoles) != len(self.prevalence):
@@ -52,6 +55,9 @@ class ModelParams:
         for i, (d, q) in enumerate(zip(self.dipoles, self.prevalence)):
             p.dipoles[i], p.prevalence[i] = float(d), float(q)
         p.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        if self.sweep_method not in _abi.SWEEP_METHODS:
+            raise ValueError("sweep_method must be one of %s" % sorted(_abi.SWEEP_METHODS))
+        p.sweep_method = _abi.SWEEP_METHODS[self.sweep_method]
         return p
 
 
@@ -358,6 +364,26 @@ class Simulation:
         a, b, n = ctypes.c_double(0.0), ctypes.c_double(0.0), ctypes.c_int(0)
         self._ck(lib().sn_gpu_phase_times(self._h, int(n_sweeps), ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)))
         return a.value, b.value, n.value
+
+    def sweep_timed(self, n: int) -> float:
+        """n sweeps; returns their device time in ms (CUDA events on the handle's stream)."""
+        ms = ctypes.c_double(0.0)
+        self._ck(lib().sn_gpu_sweep_timed(self._h, int(n), ctypes.byref(ms)))
+        return ms.value
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls of one dependency flag before a dataflow block reports SN_ERR_TIMEOUT."""
+        self._ck(lib().sn_gpu_set_wait_limit(self._h, int(polls)))
+
+    def field_cache_check(self, replica: int = 0) -> int:
+        """Entries of the cached-field sweep's cache that differ from a fresh field pass (0 = exact)."""
+        v = ctypes.c_uint64(0)
+        self._ck(lib().sn_gpu_field_cache_check(self._h, replica, ctypes.byref(v)))
+        return v.value
+
+    def test_stall_block(self, item: int) -> None:
+        """Test hook: dataflow item `item` waits on a flag nobody sets (-1 restores)."""
+        self._ck(lib().sn_gpu_test_stall_block(self._h, int(item)))
 
     def flow_stats(self) -> dict:
         """Dataflow schedule statistics since the last call (see sn_gpu_flow_stats)."""

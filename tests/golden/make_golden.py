@@ -11,8 +11,12 @@ the reference itself are what pin the CPU oracle:
                         with ACCEPT/REJECT, for several parameter sets
   ref_site_energy.npz   site_energy() values for random trial moves
   ref_equilibrium.npz   per-sweep E/site and |P|/site of random-sequential runs
-                        (statistical oracle): 32^3, cutoff 3, CageStrain 1,
-                        T in {50,150,300,500}, 4 seeds each
+                        (statistical oracle), 16 seeds per temperature, 32^3:
+                        cutoff 3 / CageStrain 1 / no field / all occupied at
+                        T in {50,150,300,500}; cutoff 3 / 30 % vacancies /
+                        Efield (0,0,0.1) at T in {150,300}; cutoff 4 /
+                        CageStrain 0.5 / Efield (0.05,0,0.05) / 10 % vacancies
+                        at T in {150,300}
   ref_analysis.npz      dipole_potential, dipole_electricfield(4),
                         dipole_electricfieldoffset(2) maps, polarisation(),
                         landau_order() and the radial_order_parameter file for
@@ -24,6 +28,7 @@ the reference itself are what pin the CPU oracle:
                         "spectrum" run with every analysis flag on and no moves
 
 Usage:  python tests/golden/make_golden.py [--skip-equilibrium] [--analysis-only]
+                                          [--equilibrium-only [case ...]]
 """
 from __future__ import annotations
 
@@ -49,9 +54,17 @@ TRAJ_CASES = [
          prevalence=(0.5, 0.3, 0.2), efield=(0.0, 0.0, 0.2), moves=8000),
 ]
 
-EQ_T = (50, 150, 300, 500)
-EQ_SEEDS = 4
-EQ_L = 32
+# Statistical oracle: three Hamiltonians, 16 independent reference runs per
+# temperature.  "plain" is the small cubic case (all sites occupied, no field);
+# "vacfield" the solid solution with vacancies zeroed after solid_solution and
+# a field along z; "rc4cage" cutoff 4 with a weaker cage strain, an oblique
+# field and 10 % vacancies.
+EQ_CASES = [
+    dict(name="plain", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.0), occupancy=1.0, T=(50, 150, 300, 500)),
+    dict(name="vacfield", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.1), occupancy=0.7, T=(150, 300)),
+    dict(name="rc4cage", L=32, cutoff=4, cage_strain=0.5, efield=(0.05, 0.0, 0.05), occupancy=0.9, T=(150, 300)),
+]
+EQ_SEEDS = 16
 EQ_EQUIL = 300
 EQ_PROD = 200
 
@@ -103,37 +116,71 @@ def site_energies(R):
 
 
 def _eq_run(args):
-    T, k = args
+    ci, T, k = args
     from oracle import oracle as O
     from oracle import ref_harness as R
-    L = EQ_L
-    seed = (0xDEADBEEF + T + 7919 * k) & 0xFFFFFFFF
-    s = R.RefSim(L, L, L, cutoff=3, T=T, seed=seed)
+    c = EQ_CASES[ci]
+    L = c["L"]
+    p = c["occupancy"]
+    lengths, prev = ((1.0,), (1.0,)) if p >= 1.0 else ((1.0, 0.0), (p, 1.0 - p))
+    # The reference's random_sphere_point tests x1*x1 + x2*x2 > 1 but takes
+    # sqrt(1 - x1*x1 - x2*x2), rounded differently: when the sum is within
+    # rounding of 1 the square root is of a negative number and the dipole is
+    # NaN (src/starrynight-config.c:209-225).  A NaN site never moves and
+    # freezes its neighbours, so such an initial lattice is redrawn with the
+    # next seed.  (Proposals with NaN are always rejected and never enter
+    # the lattice.)
+    for attempt in range(100):
+        seed = (0xDEADBEEF + T + 7919 * k + 104729 * ci + 15485863 * attempt) & 0xFFFFFFFF
+        s = R.RefSim(L, L, L, cutoff=c["cutoff"], cage_strain=c["cage_strain"], efield=c["efield"], T=T,
+                     lengths=lengths, prevalence=prev, seed=seed)
+        if np.isfinite(s.lattice()).all():
+            break
+    if p < 1.0:  # vacancies as zero vectors, as on the GPU (src/starrynight-lattice.c:139-171 sets only length)
+        lat = s.lattice()
+        lat[lat[:, 3] == 0, :3] = 0.0
+        s.set_lattice(lat)
     N = L ** 3
     s.mc_moves(EQ_EQUIL * N)
-    m = O.make_model(L, L, L, 3, T=T)
+    m = O.make_model(L, L, L, c["cutoff"], T=T, efield=c["efield"], cage_strain=c["cage_strain"])
     E, P = [], []
     for _ in range(EQ_PROD):
         s.mc_moves(N)
         lat = s.lattice()
         px, py, pz, ln = O.soa(lat)
         E.append(O.energy64(m, px, py, pz, ln)["E"] / N)
-        P.append(np.linalg.norm(lat[:, :3].astype(np.float64).sum(axis=0)) / N)
-    return T, k, np.array(E), np.array(P)
+        P.append(np.linalg.norm((lat[:, :3].astype(np.float64) * lat[:, 3:4]).sum(axis=0)) / N)
+    return ci, T, k, np.array(E), np.array(P)
 
 
-def equilibrium():
-    jobs = [(T, k) for T in EQ_T for k in range(EQ_SEEDS)]
+def equilibrium(only=None):
+    """only: names of the cases to run again; the others are kept from the existing file."""
+    keep = {}
+    path = os.path.join(HERE, "ref_equilibrium.npz")
+    if only and os.path.exists(path):
+        with np.load(path) as old:
+            keep = {k: old[k] for k in old.files}
+    jobs = [(ci, T, k) for ci, c in enumerate(EQ_CASES) for T in c["T"] for k in range(EQ_SEEDS)
+            if not only or c["name"] in only]
+    jobs.sort(key=lambda j: -EQ_CASES[j[0]]["cutoff"])  # longest runs first
     ctx = mp.get_context("spawn")
     with ctx.Pool(min(len(jobs), os.cpu_count() or 4)) as pool:
-        res = pool.map(_eq_run, jobs)
-    E = np.zeros((len(EQ_T), EQ_SEEDS, EQ_PROD))
-    P = np.zeros_like(E)
-    for T, k, e, p in res:
-        i = EQ_T.index(T)
-        E[i, k], P[i, k] = e, p
-    np.savez_compressed(os.path.join(HERE, "ref_equilibrium.npz"), T=np.array(EQ_T), E=E, P=P,
-                        L=EQ_L, equil=EQ_EQUIL, prod=EQ_PROD)
+        res = pool.map(_eq_run, jobs, chunksize=1)
+    out = dict(keep)
+    out.update({"seeds": EQ_SEEDS, "equil": EQ_EQUIL, "prod": EQ_PROD})
+    for ci, c in enumerate(EQ_CASES):
+        if only and c["name"] not in only:
+            continue
+        E = np.zeros((len(c["T"]), EQ_SEEDS, EQ_PROD))
+        P = np.zeros_like(E)
+        for cj, T, k, e, p in res:
+            if cj == ci:
+                i = c["T"].index(T)
+                E[i, k], P[i, k] = e, p
+        n = c["name"]
+        out[n + "/E"], out[n + "/P"], out[n + "/T"] = E, P, np.array(c["T"])
+        out[n + "/params"] = np.array([c["L"], c["cutoff"], c["cage_strain"], *c["efield"], c["occupancy"]])
+    np.savez_compressed(os.path.join(HERE, "ref_equilibrium.npz"), **out)
 
 
 ANALYSIS_CASES = [
@@ -249,6 +296,11 @@ def main():
     if not R.available():
         raise SystemExit("the reference harness is not built (reference tree missing?)")
     import tempfile
+    if "--equilibrium-only" in sys.argv:
+        # optional case names after the flag: run only those again
+        rest = sys.argv[sys.argv.index("--equilibrium-only") + 1:]
+        equilibrium([a for a in rest if not a.startswith("-")] or None)
+        return
     if "--analysis-only" not in sys.argv:
         neighbours(R)
         trajectories(R)

@@ -3,7 +3,7 @@ launch per block colour (SN_SCHEDULE=phases) -- make the same moves: every
 block reads and writes exactly what the per-colour order gives it, so the
 lattices and counters are bit-identical, including replica tables of mixed
 shapes, slabs, vacancies and cutoff 5, and whatever grouping of the dataflow
-queue is chosen."""
+queue is chosen -- for the stencil sweep and for the cached-field sweep."""
 import numpy as np
 import pytest
 
@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _run(sn, monkeypatch, env, params, reps, n=4):
-    for k in ("SN_SCHEDULE", "SN_FLOW_GROUP"):
+    for k in ("SN_SCHEDULE", "SN_FLOW_GROUP", "SN_SWEEP"):
         monkeypatch.delenv(k, raising=False)
     for k, v in env.items():
         monkeypatch.setenv(k, v)
@@ -37,13 +37,15 @@ def _cases(sn):
     ]
 
 
+@pytest.mark.parametrize("method", ["stencil", "cached"])
 @pytest.mark.parametrize("idx", range(4))
-def test_dataflow_equals_per_colour_launches(native_lib, monkeypatch, idx):
+def test_dataflow_equals_per_colour_launches(native_lib, monkeypatch, idx, method):
     sn = native_lib
     name, params, reps = _cases(sn)[idx]
-    a = _run(sn, monkeypatch, {"SN_SCHEDULE": "phases"}, params, reps)
+    a = _run(sn, monkeypatch, {"SN_SCHEDULE": "phases", "SN_SWEEP": method}, params, reps)
     assert a[3]["dataflow"] is False
     for env in ({}, {"SN_FLOW_GROUP": "-1"}, {"SN_FLOW_GROUP": "4"}):
+        env = dict(env, SN_SWEEP=method)
         b = _run(sn, monkeypatch, env, params, reps)
         assert b[3]["dataflow"] is True
         assert (a[0], a[1]) == (b[0], b[1]), (name, env)

@@ -80,6 +80,8 @@ def test_reference_site_energy_values():
 
 def test_equilibrium_fixture_is_sane():
     d = np.load(os.path.join(GOLD, "ref_equilibrium.npz"))
-    E = d["E"].mean(axis=(1, 2))
-    assert np.all(np.diff(E) > 0)  # energy per site rises with temperature
-    assert d["E"].shape == (len(d["T"]), 4, int(d["prod"]))
+    for case in ("plain", "vacfield", "rc4cage"):
+        E = d[case + "/E"]
+        assert E.shape == (len(d[case + "/T"]), int(d["seeds"]), int(d["prod"]))
+        assert np.isfinite(E).all() and np.isfinite(d[case + "/P"]).all()
+        assert np.all(np.diff(E.mean(axis=(1, 2))) > 0)  # energy per site rises with temperature
