@@ -312,8 +312,11 @@ bool plan_cached(SnTile &t, int Z, int rc, bool mixed, int limit, int pc_min)
     t.cH[2] = (rc + 3) / 4 * 4;
     for (int a = 0; a < 3; a++) t.cT[a] = t.B[a] + 2 * t.cH[a];
     t.cslots = t.cT[0] * t.cT[1] * t.cT[2];
-    t.cpc = t.ng;
+    // a thread draws the proposals of at most SN_CACHED_PROPS_PER_THREAD groups per chunk
+    const int pstride = SN_CACHED_THREADS / t.tg;
+    t.cpc = std::min(t.ng, SN_CACHED_PROPS_PER_THREAD * pstride);
     while (t.cpc > 1 && k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed) > limit) t.cpc--;
+    if (t.cpc > pstride) t.cpc -= t.cpc % pstride;  // whole rounds of the proposal threads
     t.csmem = k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed);
     if (t.csmem > limit || t.cpc < pc_min) return false;
     if (sn_sweep::sn_gfield_smem(t.cslots, mixed) > kSmemLimit) return false;

@@ -36,6 +36,7 @@
 #endif
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
 #define SN_CACHED_THREADS 256    // block size of the cached-field sweep kernel
+#define SN_CACHED_PROPS_PER_THREAD 4  // proposals a thread draws per staged chunk (cached sweep)
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log
 
 // Geometry of one replica's tiles: block dims, tile dims (block + halo),

@@ -551,9 +551,9 @@ struct SweepBounds {
 };
 
 template <int RC, bool TWO_D, bool MIXED, bool CACHED, bool FLOW>
-__device__ __forceinline__ void sweep_block_any(const SnWork w, const SnPhaseArgs &a, unsigned char *smem)
+__device__ __forceinline__ void sweep_block_any(const SnWork w, const SnPhaseArgs &a, unsigned char *smem, bool first)
 {
-    if constexpr (CACHED && !TWO_D) sweep_block_cached<RC, MIXED, FLOW>(w, a, smem);
+    if constexpr (CACHED && !TWO_D) sweep_block_cached<RC, MIXED, FLOW>(w, a, smem, first);
     else sweep_block<RC, TWO_D, MIXED, FLOW>(w, a, smem);
 }
 
@@ -563,7 +563,7 @@ __global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACH
     sweep_phase(const SnPhaseArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    sweep_block_any<RC, TWO_D, MIXED, CACHED, false>(a.work[blockIdx.x], a, smem);
+    sweep_block_any<RC, TWO_D, MIXED, CACHED, false>(a.work[blockIdx.x], a, smem, true);
 }
 
 __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p)
@@ -596,6 +596,7 @@ __global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACH
     __shared__ int s_item;
     const int tid = threadIdx.x;
     const uint32_t epoch = *f.base.sweep + 1u;
+    bool first = true;  // this CTA's first block (per-CTA shared-memory tables)
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(f.queue, 1u);
         __syncthreads();
@@ -621,7 +622,8 @@ __global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACH
         }
         __syncthreads();
         __threadfence();
-        sweep_block_any<RC, TWO_D, MIXED, CACHED, true>(f.base.work[item], f.base, smem);
+        sweep_block_any<RC, TWO_D, MIXED, CACHED, true>(f.base.work[item], f.base, smem, first);
+        first = false;
         __syncthreads();
         if (tid == 0) {
             __threadfence();

@@ -44,6 +44,10 @@ __host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, 
 {
     CCarve c;
     uint32_t o = 0;
+    // the pair table first: its place must not depend on the replica's tile,
+    // because a CTA fills it once for all the blocks it sweeps
+    c.pairs = o;
+    o += sn_align16((uint32_t)np * 48u);
     c.tile = o;
     o += sn_align16(3u * (uint32_t)cslots * 4u);
     c.tlen = o;
@@ -52,8 +56,6 @@ __host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, 
     o += (uint32_t)(pc * tg) * 32u;  // (p', threshold), (p_old, -) per target
     c.list = o;
     o += (uint32_t)tg * 32u;         // accepted moves of a group
-    c.pairs = o;
-    o += sn_align16((uint32_t)np * 48u);
     c.cnt = o;
     o += 16u;
     c.red = o;
@@ -138,42 +140,56 @@ __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc)
 // Copy (store = false) or write back (store = true) the tile of block w:
 // cT[0] x cT[1] rows of cT[2] consecutive z sites per array, in 16-byte
 // chunks.  Z, the block origin and the z halo are multiples of 4, so a chunk
-// never straddles the periodic wrap.
+// never straddles the periodic wrap.  The write-back covers only the sites
+// within `hz` (the cutoff) of the block along z: the rounding of the z halo
+// to 4 sites adds sites that another block may hold at the same time (the
+// disjointness of running tiles holds for the cutoff-wide halo only), so
+// chunks at the two ends of a row are written site by site.
 template <bool STORE>
 __device__ __forceinline__ void move_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, int *tile,
-                                          float *tlen, int tid, int nthreads)
+                                          float *tlen, int tid, int nthreads, int hz = 0)
 {
     const int X = R.X, Y = R.Y, Z = R.Z;
     const int T1 = Gm.cT[1], T2 = Gm.cT[2], cpr = T2 >> 2;
-    const int rows = Gm.cT[0] * T1;
     const long long N = R.n_sites;
     const int cs = Gm.cslots;
-    const int narr = tlen ? 4 : 3;
-    const int total = rows * cpr;
-    for (int idx = tid; idx < total * narr; idx += nthreads) {
-        const int arr = idx / total, rem = idx - arr * total;
-        const int row = rem / cpr, c = rem - row * cpr;
+    const int total = Gm.cT[0] * T1 * cpr;
+    const int zlo = Gm.cH[2] - hz, zhi = Gm.cH[2] + Gm.B[2] + hz;  // tile z range written back
+    // one chunk position per iteration, every array at that position
+    for (int idx = tid; idx < total; idx += nthreads) {
+        const int row = idx / cpr, c = idx - row * cpr;
         const int ux = row / T1, uy = row - ux * T1;
         const int gx = sn_wrap(w.x0 - Gm.cH[0] + ux, X), gy = sn_wrap(w.y0 - Gm.cH[1] + uy, Y);
         const int gz = sn_wrap(w.z0 - Gm.cH[2] + 4 * c, Z);
         const long long g = ((long long)gx * Y + gy) * Z + gz;
         const int slot = row * T2 + 4 * c;
-        if (arr < 3) {
-            int *src = R.gcache + arr * N + g;
-            int *dst = tile + arr * cs + slot;
-            if (STORE) {
-                *reinterpret_cast<int4 *>(src) = *reinterpret_cast<const int4 *>(dst);
+        if (STORE) {
+            if (4 * c >= zlo && 4 * c + 4 <= zhi) {
+#pragma unroll
+                for (int arr = 0; arr < 3; arr++)
+                    *reinterpret_cast<int4 *>(R.gcache + arr * N + g) =
+                        *reinterpret_cast<const int4 *>(tile + arr * cs + slot);
             } else {
-                cp_async16(dst, src);
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+                    if (4 * c + e >= zlo && 4 * c + e < zhi) {
+#pragma unroll
+                        for (int arr = 0; arr < 3; arr++) R.gcache[arr * N + g + e] = tile[arr * cs + slot + e];
+                    }
             }
-        } else if (!STORE) {
-            cp_async16(tlen + slot, R.len + g);
+        } else {
+#pragma unroll
+            for (int arr = 0; arr < 3; arr++) cp_async16(tile + arr * cs + slot, R.gcache + arr * N + g);
+            if (tlen) cp_async16(tlen + slot, R.len + g);
         }
     }
 }
 
+// fill: write the stencil pair table into shared memory (once per CTA: the
+// table depends on the cutoff only).
 template <int RC, bool MIXED, bool FLOW>
-__device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhaseArgs &a, unsigned char *smem)
+__device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhaseArgs &a, unsigned char *smem,
+                                                   bool fill)
 {
     using G = Geo<RC, false>;
     constexpr int S = G::S, NP = G::NP;
@@ -216,11 +232,13 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     move_tile<false>(R, Gm, w, tile, tlen, tid, NT);
     if (tid < 2) cnt[tid] = 0;
 
-    // this thread's target role (phase A): target tt of every colour group
-    const int tt = tid;
+    // this thread's target role: target tt of every colour group.  All
+    // threads draw proposals (thread tid for target tt = tid % tg of groups
+    // pj0, pj0 + NT/tg, ... of a chunk); threads tid < tg also finalize.
+    const int tt = tid % tg, pj0 = tid / tg, pstride = NT / tg;
     const int hh = tt / tp, t = tt - (tt / tp) * tp;
     const int qz = t % nqz, qy = (t / nqz) % nqy, qx = t / (nqz * nqy);
-    const bool tvalid = tid < tg && qx < Gm.nq[0];
+    const bool tvalid = tid < pstride * tg && qx < Gm.nq[0];
     const int trel = (S * qx * T1 + S * qy) * T2 + S * qz;
     const int srel = ((S * qx) * Y + S * qy) * Z + S * qz;
 
@@ -252,24 +270,51 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
             __syncthreads();  // previous chunk fully consumed
             gchunk = g;
             gnext = min(g + pc, ng);
-            if (tid < tg) {
-                for (int k = 0; k < gnext - g; k++) {
-                    int cx, cy, cz;
-                    group_colour<S, S, MERGE>(g + k, hh, cx, cy, cz);
+            if (tid < pstride * tg) {
+                // This thread's groups k = pj0 + i * pstride of the chunk (at most
+                // SN_CACHED_PROPS_PER_THREAD; the planner sizes pc for that): first
+                // every load, then every proposal, so the loads' latencies overlap
+                // and the independent Philox chains interleave.
+                const int nk = gnext - g;
+                int site_k[SN_CACHED_PROPS_PER_THREAD];
+                bool tgt_k[SN_CACHED_PROPS_PER_THREAD];
+                float len_k[SN_CACHED_PROPS_PER_THREAD];
+                float4 po_k[SN_CACHED_PROPS_PER_THREAD];
+#pragma unroll
+                for (int i = 0; i < SN_CACHED_PROPS_PER_THREAD; i++) {
+                    const int k = pj0 + i * pstride;
+                    tgt_k[i] = false;
+                    site_k[i] = 0;
+                    len_k[i] = 0.0f;
+                    po_k[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (k < nk) {
+                        int cx, cy, cz;
+                        group_colour<S, S, MERGE>(g + k, hh, cx, cy, cz);
+                        tgt_k[i] = (g + k < 64) ? ((amask >> (g + k)) & 1ull) != 0ull
+                                                : (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
+                                                   qz < sn_count(Bz, cz, S));
+                        site_k[i] = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
+                    }
+                    if (tgt_k[i]) {
+                        const int site = site_k[i];
+                        len_k[i] = FLOW ? __ldcg(glen + site) : glen[site];
+                        po_k[i] = make_float4(FLOW ? __ldcg(gpx + site) : gpx[site], FLOW ? __ldcg(gpy + site) : gpy[site],
+                                              FLOW ? __ldcg(gpz + site) : gpz[site], 0.0f);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < SN_CACHED_PROPS_PER_THREAD; i++) {
+                    const int k = pj0 + i * pstride;
+                    if (k >= nk) continue;
                     float4 pr = make_float4(0.0f, 0.0f, 0.0f, -2.0f);  // no target here
                     float4 po = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if ((g + k < 64) ? ((amask >> (g + k)) & 1ull)
-                                     : (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
-                                        qz < sn_count(Bz, cz, S))) {
-                        const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
+                    if (tgt_k[i]) {
                         pr.w = -1.0f;  // vacancy
-                        if ((FLOW ? __ldcg(glen + site) : glen[site]) != 0.0f) {
-                            po = make_float4(FLOW ? __ldcg(gpx + site) : gpx[site],
-                                             FLOW ? __ldcg(gpy + site) : gpy[site],
-                                             FLOW ? __ldcg(gpz + site) : gpz[site], 0.0f);
+                        if (len_k[i] != 0.0f) {
+                            po = po_k[i];
                             float3 p;
                             float u;
-                            if (!sn_proposal((uint32_t)site, sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
+                            if (!sn_proposal((uint32_t)site_k[i], sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
                                 p = make_float3(po.x, po.y, po.z);
                             // accept iff dE < -ln(u)/beta  <=>  dE < 0 || exp(-beta dE) > u
                             const float thr = u > 0.0f ? -logf(u) / beta : INFINITY;
@@ -282,8 +327,9 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
             }
             if (g == 0) {
                 // the pair table, then this thread's pairs (after the barrier below)
-                fill_pairs<RC>(std::make_integer_sequence<int, NP>{}, reinterpret_cast<CPair *>(smem + cv.pairs),
-                               tid, NT);
+                if (fill)
+                    fill_pairs<RC>(std::make_integer_sequence<int, NP>{}, reinterpret_cast<CPair *>(smem + cv.pairs),
+                                   tid, NT);
                 cp_async_wait_all();
                 __syncthreads();
 #pragma unroll
@@ -391,7 +437,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     }
 
     // ---- the tile's fields back to HBM ---------------------------------------------
-    move_tile<true>(R, Gm, w, tile, nullptr, tid, NT);
+    move_tile<true>(R, Gm, w, tile, nullptr, tid, NT, RC);
 
     // ---- the block's final sites to the caller's buffer ---------------------------
     if (float *out = R.out_xyz) {
@@ -407,12 +453,30 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     }
 
     // ---- block reduction of the move statistics ---------------------------------
-    double v[6] = {sdE.value(), sPx.value(), sPy.value(), sPz.value(), (double)sacc, (double)satt};
+    // Within a warp the compensated FP32 sums are combined as (sum, error)
+    // pairs by error-free additions (Knuth's TwoSum); FP64 (a slow pipe on this
+    // GPU) is used only to add the warps' results.
+    float hs[4] = {sdE.s, sPx.s, sPy.s, sPz.s}, hc[4] = {-sdE.c, -sPx.c, -sPy.c, -sPz.c};
+    unsigned int ia = sacc, it = satt;
 #pragma unroll
-    for (int k = 0; k < 6; k++) v[k] = warp_sum(v[k]);
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float bs = __shfl_xor_sync(0xffffffffu, hs[k], o), bc = __shfl_xor_sync(0xffffffffu, hc[k], o);
+            const float t2 = __fadd_rn(hs[k], bs);
+            const float bb = __fsub_rn(t2, hs[k]);
+            const float err = __fadd_rn(__fsub_rn(hs[k], __fsub_rn(t2, bb)), __fsub_rn(bs, bb));
+            hs[k] = t2;
+            hc[k] = __fadd_rn(__fadd_rn(hc[k], bc), err);
+        }
+        ia += __shfl_xor_sync(0xffffffffu, ia, o);
+        it += __shfl_xor_sync(0xffffffffu, it, o);
+    }
     if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < 6; k++) red[warp * 16 + k] = v[k];
+        for (int k = 0; k < 4; k++) red[warp * 16 + k] = (double)hs[k] + (double)hc[k];
+        red[warp * 16 + 4] = (double)ia;
+        red[warp * 16 + 5] = (double)it;
     }
     __syncthreads();
     if (tid < 6) {
@@ -444,14 +508,14 @@ __device__ __forceinline__ void stage_p_tile(const SnReplicaDev &R, const SnTile
     const int T1 = Gm.cT[1], T2 = Gm.cT[2], cpr = T2 >> 2;
     const int total = Gm.cT[0] * T1 * cpr;
     const int cs = Gm.cslots;
-    const float *src[4] = {R.px, R.py, R.pz, R.len};
     for (int idx = tid; idx < total * (MIXED ? 4 : 3); idx += nthreads) {
         const int arr = idx / total, rem = idx - arr * total;
         const int row = rem / cpr, c = rem - row * cpr;
         const int ux = row / T1, uy = row - ux * T1;
         const int gx = sn_wrap(w.x0 - Gm.cH[0] + ux, X), gy = sn_wrap(w.y0 - Gm.cH[1] + uy, Y);
         const int gz = sn_wrap(w.z0 - Gm.cH[2] + 4 * c, Z);
-        cp_async16(tp + arr * cs + row * T2 + 4 * c, src[arr] + (((long long)gx * Y + gy) * Z + gz));
+        const float *src = arr == 0 ? R.px : (arr == 1 ? R.py : (arr == 2 ? R.pz : R.len));
+        cp_async16(tp + arr * cs + row * T2 + 4 * c, src + (((long long)gx * Y + gy) * Z + gz));
     }
 }
 

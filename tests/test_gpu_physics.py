@@ -213,12 +213,13 @@ def test_quench_descends_on_the_sphere(native_lib):
 
 
 @pytest.mark.gpu
-def test_batched_replicas_equal_individual_runs(native_lib):
+@pytest.mark.parametrize("method", ["stencil", "cached"])
+def test_batched_replicas_equal_individual_runs(native_lib, method):
     sn = native_lib
-    params = sn.ModelParams(cutoff=3, seed=9)
+    params = sn.ModelParams(cutoff=3, seed=9, sweep_method=method)
     reps = [sn.Replica(32, 32, 32, T=100.0, efield=(0, 0, 0.1), seed=21),
             sn.Replica(48, 48, 48, T=300.0, efield=(0, 0, 0.0), seed=22),
-            sn.Replica(24, 16, 20, T=450.0, efield=(0.1, 0, 0), seed=23),
+            sn.Replica(24, 16, 24, T=450.0, efield=(0.1, 0, 0), seed=23),
             sn.Replica(40, 40, 1, T=200.0, seed=24)]
     with sn.Simulation(params, reps) as sim:
         for i in range(len(reps)):
