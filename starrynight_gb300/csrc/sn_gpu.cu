@@ -312,11 +312,9 @@ bool plan_cached(SnTile &t, int Z, int rc, bool mixed, int limit, int pc_min)
     t.cH[2] = (rc + 3) / 4 * 4;
     for (int a = 0; a < 3; a++) t.cT[a] = t.B[a] + 2 * t.cH[a];
     t.cslots = t.cT[0] * t.cT[1] * t.cT[2];
-    // a thread draws the proposals of at most SN_CACHED_PROPS_PER_THREAD groups per chunk
-    const int pstride = SN_CACHED_THREADS / t.tg;
-    t.cpc = std::min(t.ng, SN_CACHED_PROPS_PER_THREAD * pstride);
+    // proposal chunks (two buffered): up to 8 groups each, as many as fit
+    t.cpc = std::min(t.ng, 8);
     while (t.cpc > 1 && k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed) > limit) t.cpc--;
-    if (t.cpc > pstride) t.cpc -= t.cpc % pstride;  // whole rounds of the proposal threads
     t.csmem = k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed);
     if (t.csmem > limit || t.cpc < pc_min) return false;
     if (sn_sweep::sn_gfield_smem(t.cslots, mixed) > kSmemLimit) return false;
@@ -443,7 +441,8 @@ bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &ou
             t.smem_bytes = (int)sn_sweep::sn_carve(t.slots, t.tg, t.pc, NS, S, NF, mixed, 4).total;
             t.field_smem = (int)sn_sweep::sn_carve(t.slots, t.tg, 0, NS, S, NF, mixed, 8).total;
             if (t.smem_bytes > limit || t.field_smem > kSmemLimit || t.pc < pc_min) continue;
-            if (cached && !plan_cached(t, Z, rc, mixed, pass_limit - kSweepStatic, pass == 0 ? std::min(8, ng) : 1))
+            // two buffered chunks of >= 2 groups keep the proposal copies ahead of their use
+            if (cached && !plan_cached(t, Z, rc, mixed, pass_limit - kSweepStatic, std::min(2, ng)))
                 continue;
             bool seen = false;  // pass 1 meets pass 0's shapes again
             for (const SnTile &o : outs) seen |= o.B[0] == t.B[0] && o.B[1] == t.B[1] && o.B[2] == t.B[2];
@@ -644,7 +643,10 @@ struct sn_handle {
     std::vector<float *> lattice_mem;
     // cached-field sweep of the 3D replicas: their field caches (3N int32 each)
     bool cached = false;
+    int tile_copy = 0;  // cached sweep tile load: 0 = cp.async, 1 = TMA bulk copies (SN_TILE_COPY=bulk)
     std::vector<int *> gcache_mem;
+    std::vector<float4 *> prop_mem;  // the coming sweep's proposals (16 B per site)
+    int nsm = 0;
     // scratch (lazy)
     float *d_stage = nullptr;
     size_t stage_floats = 0;
@@ -798,6 +800,8 @@ SnPhaseArgs phase_args(const sn_handle *h, int off, int cnt)
     a.K = (float)h->params.K;
     a.constrain = h->params.constrain_to_x;
     a.dim = h->params.dim;
+    a.err = h->d_err;
+    a.tile_copy = h->tile_copy;
     return a;
 }
 
@@ -805,6 +809,13 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
 {
     cudaError_t e = cudaSuccess;
     size_t ev = 0;
+    if (h->cached) {
+        // the cached-field sweep takes its moves from a buffer drawn here
+        e = sn_launch_sweep_proposals(h->d_reps, h->nrep, h->d_sweep, h->params.dim, h->params.constrain_to_x, h->nsm,
+                                      h->stream);
+        if (nodes) (*nodes)++;
+        if (e != cudaSuccess) return e;
+    }
     if (h->flow) {
         for (int v = 0; v < 2 && e == cudaSuccess; v++) {
             if (!h->flow_items[v]) continue;
@@ -857,7 +868,7 @@ cudaError_t issue_sweep(sn_handle *h, uint64_t *nodes, std::vector<cudaEvent_t> 
 // Reads (and clears) the dataflow kernel's wait-timeout flag; the stream must be idle or is synchronised here.
 sn_status flow_status(sn_handle *h)
 {
-    if (!h->flow || !h->d_err) return SN_OK;
+    if (!h->d_err) return SN_OK;
     uint32_t err = 0;
     SN_CK(h, cudaMemcpyAsync(&err, h->d_err, sizeof(err), cudaMemcpyDeviceToHost, h->stream));
     SN_CK(h, cudaStreamSynchronize(h->stream));
@@ -903,6 +914,7 @@ void destroy_all(sn_handle *h)
     if (h->graph) cudaGraphExecDestroy(h->graph);
     for (float *p : h->lattice_mem) cudaFree(p);
     for (int *p : h->gcache_mem) cudaFree(p);
+    for (float4 *p : h->prop_mem) cudaFree(p);
     void *ptrs[] = {h->d_reps,  h->d_geoms, h->d_acc,   h->d_state, h->d_sweep, h->d_hist, h->d_red,
                     h->d_drift, h->d_ex,    h->d_order, h->d_flags, h->d_work,  h->d_stage, h->d_site,
                     h->d_grad,  h->d_trace, h->d_deps,  h->d_done,  h->d_queue, h->d_err,
@@ -1291,10 +1303,16 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
             R.gcache = gc;
             R.gscale = std::ldexp(1.0f, gk);
             R.ginv = std::ldexp(1.0f, -gk);
+            float4 *pb = nullptr;
+            if (cudaMalloc(&pb, (size_t)N * sizeof(float4)) != cudaSuccess)
+                return bail(fail(h, SN_ERR_NOMEM, "replica %d: cannot allocate the proposal buffer of %lld sites", r, N));
+            h->prop_mem.push_back(pb);
+            R.prop = pb;
         }
     }
 
     if (const char *env = getenv("SN_SCHEDULE")) h->flow = strcmp(env, "phases") != 0;
+    if (const char *env = getenv("SN_TILE_COPY")) h->tile_copy = strcmp(env, "bulk") == 0 ? 1 : 0;
     SnPlan plan;
     {
         std::string why;
@@ -1303,6 +1321,7 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) !=
                                                       cudaSuccess)
             nsm = 0;
+        h->nsm = nsm > 0 ? nsm : 1;
         if (!build_plan(h->tiles, replicas, n_replicas, h->flow, plan, why, nsm > 0 ? 3 * nsm : 512))
             return bail(fail(h, SN_ERR_SCHEDULE, "%s", why.c_str()));
     }
@@ -1349,8 +1368,8 @@ sn_status sn_gpu_init(const sn_params *params, int n_replicas, const sn_replica_
         ALLOC(h->d_done, (work.size() + 1) * sizeof(uint32_t));
         h->done_n = work.size();
         ALLOC(h->d_queue, 2 * sizeof(uint32_t));
-        ALLOC(h->d_err, 4 * sizeof(uint32_t));
     }
+    ALLOC(h->d_err, 4 * sizeof(uint32_t));
 #undef ALLOC
     SnExchange ex;
     memset(&ex, 0, sizeof(ex));
@@ -2030,7 +2049,7 @@ sn_status sn_gpu_phase_times(sn_handle *h, int n_sweeps, double *avg_launch_ms, 
         float sw = 0.0f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&sw, s0, s1);
         tot_sweep += sw;
-        h->launches += (uint64_t)nl + 1;
+        h->launches += (uint64_t)nl + 1 + (h->cached ? 1 : 0);
         h->sweeps++;
     }
     for (auto &x : ev) cudaEventDestroy(x);

@@ -36,7 +36,7 @@
 #endif
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
 #define SN_CACHED_THREADS 256    // block size of the cached-field sweep kernel
-#define SN_CACHED_PROPS_PER_THREAD 4  // proposals a thread draws per staged chunk (cached sweep)
+#define SN_BULK_WAIT_LIMIT (1u << 24)  // polls of the tile-copy barrier before an error is recorded
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log
 
 // Geometry of one replica's tiles: block dims, tile dims (block + halo),
@@ -93,6 +93,10 @@ struct SnReplicaDev {
     int *gcache;
     float gscale;      // 2^k: float -> fixed point
     float ginv;        // 2^-k
+    // Proposals of the coming sweep for the cached-field sweep (null: none),
+    // one per site: (p'x, p'y, p'z, threshold -ln(u)/beta), threshold < 0 at
+    // vacancies; written by the proposal kernel before each sweep.
+    float4 *prop;
 };
 
 // Per-replica sweep accumulators (zeroed at the end of every sweep).
@@ -128,6 +132,8 @@ struct SnPhaseArgs {
     float K;
     int constrain;
     int dim;
+    uint32_t *err;   // device error flags (SnFlowArgs::err): bit 1 = a tile copy wait ran out
+    int tile_copy;   // cached-field sweep tile load: 0 = 16-byte cp.async, 1 = TMA bulk row copies
 };
 
 #define SN_MAX_DEPS 28            // 1 count + up to 26 adjacent blocks (+1 spare)

@@ -1,6 +1,7 @@
 // sn_kernels.cu -- the small kernels around the sweep: lattice
 // initialisation, host-layout conversion, the end-of-sweep fold with replica
 // exchange, recompute bookkeeping and the quench step.
+#include <algorithm>
 #include <cmath>
 
 #include "../../include/sn_gpu.h"
@@ -210,6 +211,35 @@ __global__ void proposal_batch_kernel(const uint32_t *site, uint32_t sweep, uint
     out4[4 * i + 3] = u;
 }
 
+// The proposals and accept thresholds of one sweep for every site of the
+// replicas that use the cached-field sweep (blockIdx.y = replica; replicas
+// without a proposal buffer are skipped): the move the sweep will attempt at
+// each site depends only on (seed, sweep, site), so all of them are drawn
+// here with full parallelism instead of inside the sweep's block schedule.
+// Thresholds are -ln(u)/beta (accept iff dE < threshold); vacancies get -1.
+// A proposal whose Marsaglia tries all fail keeps the old dipole.
+__global__ void sweep_proposals_kernel(const SnReplicaDev *reps, const uint32_t *sweep_ctr, int dim, int constrain)
+{
+    const SnReplicaDev &R = reps[blockIdx.y];
+    float4 *out = R.prop;
+    if (!out) return;
+    const uint32_t sweep = *sweep_ctr;
+    const uint2 key = make_uint2(R.seed_lo, R.seed_hi);
+    const float beta = R.beta;
+    const long long n = R.n_sites;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float4 pr = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+        if (R.len[i] != 0.0f) {
+            float3 p;
+            float u;
+            if (!sn_proposal((uint32_t)i, sweep, SN_STREAM_SWEEP, key, dim, constrain, p, u))
+                p = make_float3(R.px[i], R.py[i], R.pz[i]);
+            pr = make_float4(p.x, p.y, p.z, u > 0.0f ? -logf(u) / beta : INFINITY);
+        }
+        out[i] = pr;
+    }
+}
+
 // FP32 FMA throughput probe: 8 independent chains per thread, no memory
 // traffic in the loop; one result per thread keeps the work live.
 __global__ void fma_peak_kernel(float *out, int iters, float a, float b)
@@ -322,5 +352,14 @@ cudaError_t sn_launch_proposal_batch(const uint32_t *site, uint32_t sweep, uint3
     if (n <= 0) return cudaSuccess;
     proposal_batch_kernel<<<(n + 255) / 256, 256, 0, st>>>(site, sweep, make_uint2(seed_lo, seed_hi), dim, constrain,
                                                            out4, n);
+    return cudaGetLastError();
+}
+
+cudaError_t sn_launch_sweep_proposals(const SnReplicaDev *reps, int nrep, const uint32_t *sweep, int dim,
+                                      int constrain, int sms, cudaStream_t st)
+{
+    if (nrep <= 0) return cudaSuccess;
+    const int bx = std::max(1, (4 * sms + nrep - 1) / nrep);
+    sweep_proposals_kernel<<<dim3(bx, nrep), 256, 0, st>>>(reps, sweep, dim, constrain);
     return cudaGetLastError();
 }

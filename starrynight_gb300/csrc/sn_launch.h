@@ -92,6 +92,10 @@ cudaError_t sn_launch_sweep_end(SnAccum *acc, SnState *state, double *hist, SnRe
                                 uint32_t *sweep, SnExchange *ex, int *order, uint32_t *queues, cudaStream_t st);
 cudaError_t sn_launch_recompute_finish(const double *red, SnState *state, const SnReplicaDev *reps, int rep,
                                        double cage, double *drift_max, int record, cudaStream_t st);
+// The coming sweep's proposals of every replica with a proposal buffer
+// (SnReplicaDev::prop); sms = multiprocessors of the device (grid sizing).
+cudaError_t sn_launch_sweep_proposals(const SnReplicaDev *reps, int nrep, const uint32_t *sweep, int dim,
+                                      int constrain, int sms, cudaStream_t st);
 // *count += number of i < n with a[i] != b[i].
 cudaError_t sn_launch_count_diff(const int *a, const int *b, long long n, unsigned long long *count, cudaStream_t st);
 cudaError_t sn_launch_quench_step(float *px, float *py, float *pz, const float *len, const float *grad,

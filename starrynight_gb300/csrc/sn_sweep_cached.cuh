@@ -53,11 +53,11 @@ __host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, 
     c.tlen = o;
     if (mixed) o += sn_align16((uint32_t)cslots * 4u);
     c.props = o;
-    o += (uint32_t)(pc * tg) * 32u;  // (p', threshold), (p_old, -) per target
+    o += (uint32_t)(2 * pc * tg) * 32u;  // two chunks of (p', threshold), (p_old, -) per target
     c.list = o;
     o += (uint32_t)tg * 32u;         // accepted moves of a group
     c.cnt = o;
-    o += 16u;
+    o += 32u;  // two group counters, the tile-copy mbarrier (bytes 8..15), its phase parity
     c.red = o;
     o += (SN_CACHED_THREADS / 32) * 16u * 8u;
     c.total = o;
@@ -137,6 +137,94 @@ __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
 }
 
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+// ---- TMA bulk copies (the tile_copy = 1 load path) ------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// One bulk copy global -> shared of `bytes` (a multiple of 16, both addresses
+// 16-byte aligned), completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait for the tile copies of phase `parity`; on time-out records
+// bit 1 in *err, then waits once more (bounded) for the copies still in
+// flight, so the CTA never leaves with its shared memory being written.
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err)
+{
+    uint32_t it = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if (++it >= SN_BULK_WAIT_LIMIT) {
+            if (err) atomicOr(err, 2u);
+            for (uint32_t k = 0; k < SN_BULK_WAIT_LIMIT && !mbar_try_wait(bar, parity); k++) __nanosleep(1000);
+            return;
+        }
+    }
+}
+
+// The tile of block w (3 field arrays, and the lengths when tlen is set) as
+// TMA bulk copies, one per tile row and array (two where the row wraps
+// around z), all completing on `bar`.  Thread 0 has announced the byte count
+// before any copy is issued.
+__device__ __forceinline__ void bulk_load_tile(const SnReplicaDev &R, const SnTile &Gm, const SnWork &w, int *tile,
+                                               float *tlen, uint64_t *bar, int tid, int nthreads)
+{
+    const int X = R.X, Y = R.Y, Z = R.Z;
+    const int T1 = Gm.cT[1], T2 = Gm.cT[2];
+    const long long N = R.n_sites;
+    const int cs = Gm.cslots;
+    const int rows = Gm.cT[0] * T1;
+    const int narr = tlen ? 4 : 3;
+    const int zs = sn_wrap(w.z0 - Gm.cH[2], Z);
+    const int n1 = min(T2, Z - zs);  // sites before the z wrap (multiples of 4)
+    asm volatile("fence.proxy.async;\n" ::: "memory");
+    for (int i = tid; i < rows * narr; i += nthreads) {
+        const int arr = i / rows, row = i - arr * rows;
+        const int ux = row / T1, uy = row - ux * T1;
+        const int gx = sn_wrap(w.x0 - Gm.cH[0] + ux, X), gy = sn_wrap(w.y0 - Gm.cH[1] + uy, Y);
+        const long long gr = ((long long)gx * Y + gy) * Z;
+        const void *src = arr < 3 ? (const void *)(R.gcache + arr * N + gr) : (const void *)(R.len + gr);
+        unsigned char *dst = arr < 3 ? (unsigned char *)(tile + arr * cs + row * T2) : (unsigned char *)(tlen + row * T2);
+        bulk_g2s(dst, (const unsigned char *)src + 4ll * zs, 4u * n1, bar);
+        if (n1 < T2) bulk_g2s(dst + 4 * n1, src, 4u * (T2 - n1), bar);
+    }
+}
+
+// Wait until at most N of this thread's committed copy groups are in flight.
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // Copy (store = false) or write back (store = true) the tile of block w:
 // cT[0] x cT[1] rows of cT[2] consecutive z sites per array, in 16-byte
 // chunks.  Z, the block origin and the z halo are multiples of 4, so a chunk
@@ -153,18 +241,24 @@ __device__ __forceinline__ void move_tile(const SnReplicaDev &R, const SnTile &G
     const int T1 = Gm.cT[1], T2 = Gm.cT[2], cpr = T2 >> 2;
     const long long N = R.n_sites;
     const int cs = Gm.cslots;
-    const int total = Gm.cT[0] * T1 * cpr;
+    const int rows = Gm.cT[0] * T1;
     const int zlo = Gm.cH[2] - hz, zhi = Gm.cH[2] + Gm.B[2] + hz;  // tile z range written back
-    // one chunk position per iteration, every array at that position
-    for (int idx = tid; idx < total; idx += nthreads) {
-        const int row = idx / cpr, c = idx - row * cpr;
-        const int ux = row / T1, uy = row - ux * T1;
+    // Thread tid moves chunk c of rows r0, r0 + step, ...: the chunk and the
+    // global z of a thread never change, the row advances by a fixed step
+    // (tracked as (ux, uy) without divisions).
+    const int per = nthreads / cpr;  // rows a pass covers
+    if (tid >= per * cpr) return;
+    const int c = tid % cpr, r0 = tid / cpr;
+    const int gz = sn_wrap(w.z0 - Gm.cH[2] + 4 * c, Z);
+    const bool full = 4 * c >= zlo && 4 * c + 4 <= zhi;
+    const int sx = per / T1, sy = per - (per / T1) * T1;
+    int ux = r0 / T1, uy = r0 - (r0 / T1) * T1;
+    for (int row = r0; row < rows; row += per) {
         const int gx = sn_wrap(w.x0 - Gm.cH[0] + ux, X), gy = sn_wrap(w.y0 - Gm.cH[1] + uy, Y);
-        const int gz = sn_wrap(w.z0 - Gm.cH[2] + 4 * c, Z);
         const long long g = ((long long)gx * Y + gy) * Z + gz;
         const int slot = row * T2 + 4 * c;
         if (STORE) {
-            if (4 * c >= zlo && 4 * c + 4 <= zhi) {
+            if (full) {
 #pragma unroll
                 for (int arr = 0; arr < 3; arr++)
                     *reinterpret_cast<int4 *>(R.gcache + arr * N + g) =
@@ -181,6 +275,12 @@ __device__ __forceinline__ void move_tile(const SnReplicaDev &R, const SnTile &G
 #pragma unroll
             for (int arr = 0; arr < 3; arr++) cp_async16(tile + arr * cs + slot, R.gcache + arr * N + g);
             if (tlen) cp_async16(tlen + slot, R.len + g);
+        }
+        ux += sx;
+        uy += sy;
+        if (uy >= T1) {
+            uy -= T1;
+            ux++;
         }
     }
 }
@@ -211,9 +311,6 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     const int T1 = Gm.cT[1], T2 = Gm.cT[2];
     const int tp = Gm.tp, tg = Gm.tg, ng = Gm.ng, pc = Gm.cpc;
     const int nqy = Gm.nq[1], nqz = Gm.nq[2];
-    const uint32_t sweep = *a.sweep;
-    const uint2 key = make_uint2(R.seed_lo, R.seed_hi);
-    const float beta = R.beta;
     const float Ex = R.E[0], Ey = R.E[1], Ez = R.E[2];
     const float C = a.cage, Kk = a.K;
     const float Lu = R.length;
@@ -229,11 +326,28 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     int *cnt = reinterpret_cast<int *>(smem + cv.cnt);
     double *red = reinterpret_cast<double *>(smem + cv.red);
 
-    move_tile<false>(R, Gm, w, tile, tlen, tid, NT);
+    uint64_t *tbar = reinterpret_cast<uint64_t *>(cnt + 2);  // 8-byte aligned: cnt is 16-byte aligned
+    uint32_t tphase = 0;
+    if (a.tile_copy) {
+        // the tile through TMA bulk copies on an mbarrier (one phase per block)
+        if (fill && tid == 0) {
+            mbar_init(tbar, 1);
+            cnt[4] = 0;  // phase parity of the barrier's next completion
+        }
+        __syncthreads();
+        tphase = (uint32_t)cnt[4];
+        if (tid == 0)
+            mbar_arrive_expect_tx(tbar, (uint32_t)((MIXED ? 4 : 3) * Gm.cslots) * 4u);
+        __syncthreads();
+        bulk_load_tile(R, Gm, w, tile, tlen, tbar, tid, NT);
+    } else {
+        move_tile<false>(R, Gm, w, tile, tlen, tid, NT);
+    }
+    cp_async_commit();
     if (tid < 2) cnt[tid] = 0;
 
     // this thread's target role: target tt of every colour group.  All
-    // threads draw proposals (thread tid for target tt = tid % tg of groups
+    // threads stage proposals (thread tid for target tt = tid % tg of groups
     // pj0, pj0 + NT/tg, ... of a chunk); threads tid < tg also finalize.
     const int tt = tid % tg, pj0 = tid / tg, pstride = NT / tg;
     const int hh = tt / tp, t = tt - (tt / tp) * tp;
@@ -256,7 +370,6 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     KahanF sdE, sPx, sPy, sPz;
     unsigned int sacc = 0, satt = 0;
 
-    int gchunk = 0, gnext = 0;
     unsigned long long amask = 0ull;
     for (int g = 0; g < ng && g < 64; g++) {
         int cx, cy, cz;
@@ -264,74 +377,54 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         if (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) && qz < sn_count(Bz, cz, S))
             amask |= 1ull << g;
     }
-    for (int g = 0; g < ng; g++) {
-        // ---- proposals, thresholds and old dipoles of the next pc groups ----------
-        if (g == gnext) {
-            __syncthreads();  // previous chunk fully consumed
-            gchunk = g;
-            gnext = min(g + pc, ng);
-            if (tid < pstride * tg) {
-                // This thread's groups k = pj0 + i * pstride of the chunk (at most
-                // SN_CACHED_PROPS_PER_THREAD; the planner sizes pc for that): first
-                // every load, then every proposal, so the loads' latencies overlap
-                // and the independent Philox chains interleave.
-                const int nk = gnext - g;
-                int site_k[SN_CACHED_PROPS_PER_THREAD];
-                bool tgt_k[SN_CACHED_PROPS_PER_THREAD];
-                float len_k[SN_CACHED_PROPS_PER_THREAD];
-                float4 po_k[SN_CACHED_PROPS_PER_THREAD];
-#pragma unroll
-                for (int i = 0; i < SN_CACHED_PROPS_PER_THREAD; i++) {
-                    const int k = pj0 + i * pstride;
-                    tgt_k[i] = false;
-                    site_k[i] = 0;
-                    len_k[i] = 0.0f;
-                    po_k[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (k < nk) {
-                        int cx, cy, cz;
-                        group_colour<S, S, MERGE>(g + k, hh, cx, cy, cz);
-                        tgt_k[i] = (g + k < 64) ? ((amask >> (g + k)) & 1ull) != 0ull
-                                                : (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
-                                                   qz < sn_count(Bz, cz, S));
-                        site_k[i] = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
-                    }
-                    if (tgt_k[i]) {
-                        const int site = site_k[i];
-                        len_k[i] = FLOW ? __ldcg(glen + site) : glen[site];
-                        po_k[i] = make_float4(FLOW ? __ldcg(gpx + site) : gpx[site], FLOW ? __ldcg(gpy + site) : gpy[site],
-                                              FLOW ? __ldcg(gpz + site) : gpz[site], 0.0f);
-                    }
-                }
-#pragma unroll
-                for (int i = 0; i < SN_CACHED_PROPS_PER_THREAD; i++) {
-                    const int k = pj0 + i * pstride;
-                    if (k >= nk) continue;
-                    float4 pr = make_float4(0.0f, 0.0f, 0.0f, -2.0f);  // no target here
-                    float4 po = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (tgt_k[i]) {
-                        pr.w = -1.0f;  // vacancy
-                        if (len_k[i] != 0.0f) {
-                            po = po_k[i];
-                            float3 p;
-                            float u;
-                            if (!sn_proposal((uint32_t)site_k[i], sweep, SN_STREAM_SWEEP, key, a.dim, a.constrain, p, u))
-                                p = make_float3(po.x, po.y, po.z);
-                            // accept iff dE < -ln(u)/beta  <=>  dE < 0 || exp(-beta dE) > u
-                            const float thr = u > 0.0f ? -logf(u) / beta : INFINITY;
-                            pr = make_float4(p.x, p.y, p.z, thr);
-                        }
-                    }
-                    props[2 * (k * tg + tt)] = pr;
-                    props[2 * (k * tg + tt) + 1] = po;
+
+    // Proposals arrive in chunks of pc colour groups, copied asynchronously
+    // from the sweep's proposal buffer (drawn before the sweep by
+    // sweep_proposals_kernel) together with the targets' current dipoles,
+    // into two alternating buffers: chunk c + 1 is in flight while chunk c
+    // is used.
+    const int nchunks = (ng + pc - 1) / pc;
+    auto stage = [&](int c) {
+        const int g0 = c * pc, nk = min(pc, ng - g0);
+        float4 *buf = props + (c & 1) * (2 * pc * tg);
+        if (tid < pstride * tg) {
+            for (int k = pj0; k < nk; k += pstride) {
+                int cx, cy, cz;
+                group_colour<S, S, MERGE>(g0 + k, hh, cx, cy, cz);
+                const bool tgt = (g0 + k < 64) ? ((amask >> (g0 + k)) & 1ull) != 0ull
+                                               : (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) &&
+                                                  qz < sn_count(Bz, cz, S));
+                float4 *slot = buf + 2 * (k * tg + tt);
+                if (tgt) {
+                    const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
+                    cp_async16(slot, R.prop + site);
+                    cp_async4(&slot[1].x, gpx + site);
+                    cp_async4(&slot[1].y, gpy + site);
+                    cp_async4(&slot[1].z, gpz + site);
+                } else {
+                    slot[0] = make_float4(0.0f, 0.0f, 0.0f, -2.0f);  // no target here
                 }
             }
+        }
+        cp_async_commit();
+    };
+    stage(0);
+    const float4 *cur = props;
+    int gchunk = 0, c = -1, gnext = 0;  // chunk of the current group, first group of the next chunk
+    for (int g = 0; g < ng; g++) {
+        if (g == gnext) {
+            c++;
+            gnext = g + pc;
+            if (c + 1 < nchunks) stage(c + 1);  // into the buffer chunk c - 1 used (all done with it)
+            else cp_async_commit();
+            cp_async_wait_group<1>();  // the tile and chunk c have landed (chunk c + 1 may be in flight)
+            if (g == 0 && a.tile_copy) mbar_wait_bounded(tbar, tphase, a.err);
+            if (g == 0 && fill)
+                fill_pairs<RC>(std::make_integer_sequence<int, NP>{}, reinterpret_cast<CPair *>(smem + cv.pairs), tid,
+                               NT);
+            __syncthreads();
             if (g == 0) {
-                // the pair table, then this thread's pairs (after the barrier below)
-                if (fill)
-                    fill_pairs<RC>(std::make_integer_sequence<int, NP>{}, reinterpret_cast<CPair *>(smem + cv.pairs),
-                                   tid, NT);
-                cp_async_wait_all();
-                __syncthreads();
+                // this thread's stencil pairs for the scatter
 #pragma unroll
                 for (int k = 0; k < PPT; k++) {
                     const int q = pq + k * NT;
@@ -343,7 +436,8 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                     for (int e = 0; e < 6; e++) Tq[k][e] = P.t[e];
                 }
             }
-            __syncthreads();
+            gchunk = g;
+            cur = props + (c & 1) * (2 * pc * tg);
         }
 
         // ---- A. targets of the group: dE from the cached field, accept, record ---------
@@ -353,9 +447,9 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         if (tid < tg) {
             int cx, cy, cz;
             group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
-            const float4 pr = props[2 * ((g - gchunk) * tg + tt)];
+            const float4 pr = cur[2 * ((g - gchunk) * tg + tt)];
             if (pr.w >= 0.0f) {
-                const float4 po = props[2 * ((g - gchunk) * tg + tt) + 1];
+                const float4 po = cur[2 * ((g - gchunk) * tg + tt) + 1];
                 tslot = ((cx + Gm.cH[0]) * T1 + (cy + Gm.cH[1])) * T2 + cz + Gm.cH[2] + trel;
                 const float gx = fmaf((float)tile[tslot], ginv, Ex);
                 const float gy = fmaf((float)tile[cs + tslot], ginv, Ey);
@@ -388,8 +482,8 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
             base = __shfl_sync(0xffffffffu, base, 0);
             if (acc) {
                 const int e = base + __popc(m & ((1u << lane) - 1u));
-                const float4 pr = props[2 * ((g - gchunk) * tg + tt)];
-                const float4 po = props[2 * ((g - gchunk) * tg + tt) + 1];
+                const float4 pr = cur[2 * ((g - gchunk) * tg + tt)];
+                const float4 po = cur[2 * ((g - gchunk) * tg + tt) + 1];
                 list[2 * e] = make_float4(__int_as_float(tslot), pr.x, pr.y, pr.z);
                 list[2 * e + 1] = make_float4(po.x, po.y, po.z, Li);
             }
@@ -479,6 +573,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         red[warp * 16 + 5] = (double)it;
     }
     __syncthreads();
+    if (a.tile_copy && tid == 0) cnt[4] = (int)(tphase ^ 1u);  // read by the CTA's next block after its barriers
     if (tid < 6) {
         double s = 0.0;
         for (int q = 0; q < (NT >> 5); q++) s += red[q * 16 + tid];

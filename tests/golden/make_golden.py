@@ -13,10 +13,11 @@ the reference itself are what pin the CPU oracle:
   ref_equilibrium.npz   per-sweep E/site and |P|/site of random-sequential runs
                         (statistical oracle), 16 seeds per temperature, 32^3:
                         cutoff 3 / CageStrain 1 / no field / all occupied at
-                        T in {50,150,300,500}; cutoff 3 / 30 % vacancies /
+                        T in {500,700,1000}; cutoff 3 / 30 % vacancies /
                         Efield (0,0,0.1) at T in {150,300}; cutoff 4 /
                         CageStrain 0.5 / Efield (0.05,0,0.05) / 10 % vacancies
-                        at T in {150,300}
+                        at T in {150,300}; 200 production sweeps after a
+                        per-temperature equilibration
   ref_analysis.npz      dipole_potential, dipole_electricfield(4),
                         dipole_electricfieldoffset(2) maps, polarisation(),
                         landau_order() and the radial_order_parameter file for
@@ -57,15 +58,23 @@ TRAJ_CASES = [
 # Statistical oracle: three Hamiltonians, 16 independent reference runs per
 # temperature.  "plain" is the small cubic case (all sites occupied, no field);
 # "vacfield" the solid solution with vacancies zeroed after solid_solution and
-# a field along z; "rc4cage" cutoff 4 with a weaker cage strain, an oblique
-# field and 10 % vacancies.
+# a field along z (the physics of the 256^3 benchmark lattice); "rc4cage"
+# cutoff 4 with a weaker cage strain, an oblique field and 10 % vacancies.
+# Equilibration lengths come from long single reference runs: below 500 K the
+# plain lattice keeps ordering slowly (its energy per site still falls by
+# ~0.01 per 100 sweeps after 3000 sweeps at 300 K), so it has no equilibrium
+# to compare within any affordable run and is sampled at 500-1000 K; the
+# vacancy lattice at 150 K settles after about 2000 sweeps.  The test checks
+# that every series it compares is stationary.
 EQ_CASES = [
-    dict(name="plain", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.0), occupancy=1.0, T=(50, 150, 300, 500)),
-    dict(name="vacfield", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.1), occupancy=0.7, T=(150, 300)),
-    dict(name="rc4cage", L=32, cutoff=4, cage_strain=0.5, efield=(0.05, 0.0, 0.05), occupancy=0.9, T=(150, 300)),
+    dict(name="plain", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.0), occupancy=1.0, T=(500, 700, 1000),
+         equil=(500, 500, 500)),
+    dict(name="vacfield", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.1), occupancy=0.7, T=(150, 300),
+         equil=(2500, 500)),
+    dict(name="rc4cage", L=32, cutoff=4, cage_strain=0.5, efield=(0.05, 0.0, 0.05), occupancy=0.9, T=(150, 300),
+         equil=(2500, 500)),
 ]
 EQ_SEEDS = 16
-EQ_EQUIL = 300
 EQ_PROD = 200
 
 
@@ -141,7 +150,7 @@ def _eq_run(args):
         lat[lat[:, 3] == 0, :3] = 0.0
         s.set_lattice(lat)
     N = L ** 3
-    s.mc_moves(EQ_EQUIL * N)
+    s.mc_moves(c["equil"][c["T"].index(T)] * N)
     m = O.make_model(L, L, L, c["cutoff"], T=T, efield=c["efield"], cage_strain=c["cage_strain"])
     E, P = [], []
     for _ in range(EQ_PROD):
@@ -162,12 +171,13 @@ def equilibrium(only=None):
             keep = {k: old[k] for k in old.files}
     jobs = [(ci, T, k) for ci, c in enumerate(EQ_CASES) for T in c["T"] for k in range(EQ_SEEDS)
             if not only or c["name"] in only]
-    jobs.sort(key=lambda j: -EQ_CASES[j[0]]["cutoff"])  # longest runs first
+    # longest runs first
+    jobs.sort(key=lambda j: -EQ_CASES[j[0]]["cutoff"] * EQ_CASES[j[0]]["equil"][EQ_CASES[j[0]]["T"].index(j[1])])
     ctx = mp.get_context("spawn")
     with ctx.Pool(min(len(jobs), os.cpu_count() or 4)) as pool:
         res = pool.map(_eq_run, jobs, chunksize=1)
     out = dict(keep)
-    out.update({"seeds": EQ_SEEDS, "equil": EQ_EQUIL, "prod": EQ_PROD})
+    out.update({"seeds": EQ_SEEDS, "prod": EQ_PROD})
     for ci, c in enumerate(EQ_CASES):
         if only and c["name"] not in only:
             continue
@@ -179,6 +189,7 @@ def equilibrium(only=None):
                 E[i, k], P[i, k] = e, p
         n = c["name"]
         out[n + "/E"], out[n + "/P"], out[n + "/T"] = E, P, np.array(c["T"])
+        out[n + "/equil"] = np.array(c["equil"])
         out[n + "/params"] = np.array([c["L"], c["cutoff"], c["cage_strain"], *c["efield"], c["occupancy"]])
     np.savez_compressed(os.path.join(HERE, "ref_equilibrium.npz"), **out)
 

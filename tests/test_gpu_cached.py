@@ -130,3 +130,30 @@ def test_refusals(native_lib):
         sim.upload(0, xyz)
         sim.sweep(2)
         assert sim.field_cache_check(0) == 0
+
+
+@pytest.mark.parametrize("kw", [dict(cutoff=3, efield=(0.0, 0.0, 0.1), dipoles=(1.0, 0.0), prevalence=(0.7, 0.3)),
+                                dict(cutoff=3, dipoles=(1.0, 0.6, 0.0), prevalence=(0.5, 0.3, 0.2)),
+                                dict(cutoff=5, K=0.2)], ids=["vacancy_field", "mixture", "rc5"])
+def test_tma_bulk_tile_load_equals_async_copies(native_lib, monkeypatch, kw):
+    """The tile load by TMA bulk row copies on an mbarrier (SN_TILE_COPY=bulk)
+    moves the same bytes as the 16-byte cp.async path: identical lattices,
+    counters and caches, for both sweep schedules."""
+    sn = native_lib
+    shape = (48, 48, 48) if kw["cutoff"] == 5 else (32, 48, 32)
+    reps = [sn.Replica(*shape, T=200.0, seed=3), sn.Replica(*shape, T=400.0, seed=4)]
+    out = {}
+    for copy in ("async", "bulk"):
+        for sched in ("flow", "phases"):
+            monkeypatch.setenv("SN_TILE_COPY", copy)
+            monkeypatch.setenv("SN_SCHEDULE", sched)
+            with sn.Simulation(_params(sn, seed=11, **kw), reps) as sim:
+                for r in range(len(reps)):
+                    sim.init_lattice(r)
+                acc = sim.sweep(6, counts=True)
+                assert all(sim.field_cache_check(r) == 0 for r in range(len(reps)))
+                out[copy, sched] = (acc, [sim.download(r)[0] for r in range(len(reps))])
+    ref = out["async", "flow"]
+    for k, v in out.items():
+        assert v[0] == ref[0], k
+        assert all(np.array_equal(a, b) for a, b in zip(v[1], ref[1])), k

@@ -3,10 +3,12 @@ reference's own random-sequential runs.
 
 tests/golden/ref_equilibrium.npz holds per-sweep E/site and |P|/site of the
 unmodified reference (MT19937, MC_move, src/starrynight-montecarlo-core.c:
-143-191) on 32^3 lattices, 16 independent seeds per temperature, after 300
-equilibration sweeps (tests/golden/make_golden.py), for three Hamiltonians:
+143-191) on 32^3 lattices, 16 independent seeds per temperature, 200
+production sweeps after a per-temperature equilibration of 500 or 2500
+sweeps (tests/golden/make_golden.py), for three Hamiltonians:
   plain     cutoff 3, CageStrain 1, no field, every site occupied,
-            T in {50, 150, 300, 500} K;
+            T in {500, 700, 1000} K (below 500 K this lattice keeps ordering
+            for thousands of sweeps: it has no equilibrium within reach);
   vacfield  cutoff 3, CageStrain 1, 30 % vacancies zeroed after
             solid_solution (src/starrynight-lattice.c:139-171), Efield
             (0, 0, 0.1) (src/starrynight-montecarlo-core.c:120-121), T in
@@ -14,7 +16,9 @@ equilibration sweeps (tests/golden/make_golden.py), for three Hamiltonians:
   rc4cage   cutoff 4, CageStrain 0.5, Efield (0.05, 0, 0.05), 10 % vacancies,
             T in {150, 300} K.
 The colour sweep satisfies detailed balance with the same stationary
-distribution, so equilibrium averages -- not trajectories -- must agree.
+distribution, so equilibrium averages -- not trajectories -- must agree, and
+only where both sides are in equilibrium: every compared series must be
+stationary (its second half agrees with its first half within 3 sigma).
 
 Error bars: each run (one seed) is one block; the runs are independent, so
 the standard error of a side's mean is the spread of its run means
@@ -62,6 +66,13 @@ def compare(gpu, ref):
     return mg - mr, float(np.hypot(sg, sr))
 
 
+def drift(runs):
+    """(second-half mean - first-half mean, its standard error) over independent runs."""
+    h = runs.shape[-1] // 2
+    dd = runs[..., h:].mean(axis=-1) - runs[..., :h].mean(axis=-1)
+    return dd.mean(), dd.std(ddof=1) / np.sqrt(dd.size)
+
+
 def test_fixture_holds_every_case():
     d = np.load(GOLD)
     assert int(d["seeds"]) >= 16
@@ -69,13 +80,24 @@ def test_fixture_holds_every_case():
         E, P, T = d[c + "/E"], d[c + "/P"], d[c + "/T"]
         assert E.shape == P.shape == (len(T), int(d["seeds"]), int(d["prod"]))
         assert np.isfinite(E).all() and np.isfinite(P).all()
+        assert d[c + "/equil"].shape == T.shape
+
+
+def test_reference_runs_are_stationary():
+    """The reference's own production series are in equilibrium: no drift of
+    E/site between their two halves beyond 3 standard errors."""
+    d = np.load(GOLD)
+    for c in CASES:
+        for i, T in enumerate(d[c + "/T"]):
+            m, se = drift(d[c + "/E"][i])
+            assert abs(m) < N_SIGMA * se, (c, int(T), m, se)
 
 
 def test_compare_detects_a_planted_bias():
     """The 3-sigma test on the reference's own runs: two halves of the seeds
     agree, and a bias of 5 standard errors planted in one half is caught."""
     d = np.load(GOLD)
-    E = d["plain/E"][2]  # 300 K
+    E = d["plain/E"][0]  # 500 K
     a, b = E[: E.shape[0] // 2], E[E.shape[0] // 2:]
     diff, sig = compare(a, b)
     assert abs(diff) < N_SIGMA * sig
@@ -89,12 +111,17 @@ def test_compare_detects_a_planted_bias():
 def test_equilibrium_matches_reference_runs(native_lib, case):
     sn = native_lib
     d = np.load(GOLD)
-    equil, prod = int(d["equil"]), int(d["prod"])
+    # the GPU side equilibrates at least as long as the reference did at any
+    # of the case's temperatures (all its replicas share one handle)
+    equil, prod = int(d[case + "/equil"].max()), int(d["prod"])
     L, cutoff, cage, ex, ey, ez, occ = [float(v) for v in d[case + "/params"]]
     Ts = [int(t) for t in d[case + "/T"]]
     E, P = _gpu_runs(sn, int(L), int(cutoff), cage, (ex, ey, ez), occ, Ts, equil, prod, CASES.index(case))
     bad = []
     for i, T in enumerate(Ts):
+        m, se = drift(E[i])
+        if not abs(m) < N_SIGMA * se:
+            bad.append((T, "GPU E/site not stationary", m, se))
         for name, g, r in (("E/site", E[i], d[case + "/E"][i]), ("|P|/site", P[i], d[case + "/P"][i])):
             diff, sig = compare(g, r)
             if not abs(diff) < N_SIGMA * sig:
