@@ -45,16 +45,39 @@ def tune(params: ModelParams, replica: Replica, max_candidates: int = 6, sweeps:
     return best, results
 
 
+def _build_id() -> str:
+    """The GPU and the library build a tuned shape was measured on: a shape
+    tuned on another device or an older kernel is not reused."""
+    import hashlib
+    import os
+    from ._abi import library_path
+    gpu = "cpu"
+    try:
+        import torch
+        if torch.cuda.is_available():
+            gpu = torch.cuda.get_device_name().replace(" ", "_")
+    except Exception:
+        pass
+    h = hashlib.sha1()
+    try:
+        with open(library_path(), "rb") as f:
+            h.update(f.read())
+    except OSError:
+        h.update(b"unbuilt")
+    return "%s/%s" % (gpu, h.hexdigest()[:12])
+
+
 def _cache_key(params: ModelParams, r: Replica) -> str:
-    return "%dx%dx%d/rc%d/%s" % (r.X, r.Y, r.Z, int(params.cutoff), "mixed" if _mixed(params) else "uniform")
+    return "%s/%dx%dx%d/rc%d/%s/%s" % (_build_id(), r.X, r.Y, r.Z, int(params.cutoff),
+                                      "mixed" if _mixed(params) else "uniform", params.sweep_method)
 
 
 def tune_table(params: ModelParams, replicas: Sequence[Replica], cache: str | None = None, **kw) -> list:
     """The table with each replica's block shape tuned (once per distinct size).
 
-    cache: a JSON file of earlier choices (lattice size, cutoff, mixed or
-    uniform lengths -> block shape) on this machine; sizes found there are
-    not timed again, new choices are added to it."""
+    cache: a JSON file of earlier choices (GPU and library build, lattice
+    size, cutoff, mixed or uniform lengths, sweep method -> block shape);
+    sizes found there are not timed again, new choices are added to it."""
     import json
     import os
     known = {}

@@ -378,6 +378,8 @@ bool plan_tiles(int X, int Y, int Z, int rc, bool mixed, std::vector<SnTile> &ou
     };
     std::sort(all.begin(), all.end(), [&](const Cand &a, const Cand &b) {
         if (a.vol != b.vol) return a.vol > b.vol;
+        // the cached-field sweep moves whole z rows (16-byte chunks): longer rows first (measured faster)
+        if (cached && a.B[2] != b.B[2]) return a.B[2] > b.B[2];
         if (tile_sites(a) != tile_sites(b)) return tile_sites(a) < tile_sites(b);
         if (a.balanced != b.balanced) return a.balanced > b.balanced;
         if (a.B[2] != b.B[2]) return a.B[2] > b.B[2];

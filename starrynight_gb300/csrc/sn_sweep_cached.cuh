@@ -535,13 +535,15 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
 
     // ---- the block's final sites to the caller's buffer ---------------------------
     if (float *out = R.out_xyz) {
+        // a block row (fixed x, y) is 3*Bz consecutive floats of the interleaved
+        // buffer: lanes write consecutive floats, reading the component arrays
         for (int row = warp; row < Bx * By; row += NT >> 5) {
             const int lx = row / By, ly = row - (row / By) * By;
             const long long s0 = (((long long)(w.x0 + lx)) * Y + (w.y0 + ly)) * Z + w.z0;
-            for (int e = lane; e < Bz; e += 32) {
-                out[3 * (s0 + e) + 0] = __ldcg(gpx + s0 + e);
-                out[3 * (s0 + e) + 1] = __ldcg(gpy + s0 + e);
-                out[3 * (s0 + e) + 2] = __ldcg(gpz + s0 + e);
+            for (int e = lane; e < 3 * Bz; e += 32) {
+                const int site = e / 3, comp = e - 3 * (e / 3);
+                const float *src = comp == 0 ? gpx : (comp == 1 ? gpy : gpz);
+                out[3 * s0 + e] = __ldcg(src + s0 + site);
             }
         }
     }

@@ -25,12 +25,13 @@ def test_tune_table_once_per_size_and_cache(tmp_path, monkeypatch, native_lib):
     assert out[0].block == out[2].block and out[1].block is not None
     assert [r.T for r in out] == [100.0, 200.0, 300.0]
     saved = json.load(open(cache))
-    assert set(saved) == {"32x32x32/rc3/uniform", "48x48x48/rc3/uniform"}
+    bid = autotune._build_id()
+    assert set(saved) == {bid + "/32x32x32/rc3/uniform/auto", bid + "/48x48x48/rc3/uniform/auto"}
     # a second table: known sizes come from the cache, only the new one is timed
     calls.clear()
     out2 = autotune.tune_table(params, [sn.Replica(48, 48, 48), sn.Replica(64, 64, 64)], cache=cache)
     assert calls == [(64, 64, 64)]
-    assert out2[0].block == tuple(saved["48x48x48/rc3/uniform"])
+    assert out2[0].block == tuple(saved[bid + "/48x48x48/rc3/uniform/auto"])
     assert len(json.load(open(cache))) == 3
     # another cutoff is another key
     calls.clear()

@@ -4,7 +4,7 @@ reference's own random-sequential runs.
 tests/golden/ref_equilibrium.npz holds per-sweep E/site and |P|/site of the
 unmodified reference (MT19937, MC_move, src/starrynight-montecarlo-core.c:
 143-191) on 32^3 lattices, 16 independent seeds per temperature, 200
-production sweeps after a per-temperature equilibration of 500 or 2500
+production sweeps after a per-temperature equilibration of 500 to 3000
 sweeps (tests/golden/make_golden.py), for three Hamiltonians:
   plain     cutoff 3, CageStrain 1, no field, every site occupied,
             T in {500, 700, 1000} K (below 500 K this lattice keeps ordering
@@ -14,7 +14,7 @@ sweeps (tests/golden/make_golden.py), for three Hamiltonians:
             (0, 0, 0.1) (src/starrynight-montecarlo-core.c:120-121), T in
             {150, 300} K;
   rc4cage   cutoff 4, CageStrain 0.5, Efield (0.05, 0, 0.05), 10 % vacancies,
-            T in {150, 300} K.
+            T in {200, 300} K.
 The colour sweep satisfies detailed balance with the same stationary
 distribution, so equilibrium averages -- not trajectories -- must agree, and
 only where both sides are in equilibrium: every compared series must be
