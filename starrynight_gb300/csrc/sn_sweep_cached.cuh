@@ -84,15 +84,20 @@ __device__ __forceinline__ uint32_t q_bits(float v, float scale) { return __floa
 // t (xx yy zz xy xz yz), as the raw magic-biased bits of Q(c) per component.
 // Every kernel that builds or updates the field cache calls this function, so
 // the rounding is the same everywhere.
+// W1: w is known to be 1 (uniform lengths of 1), and the multiplication by it,
+// which is exact, is skipped.
+template <bool W1 = false>
 __device__ __forceinline__ void q_contrib(const float (&t)[6], bool NN, float w, float C, float scale, float px,
                                           float py, float pz, uint32_t &qx, uint32_t &qy, uint32_t &qz)
 {
     float vx = fmaf(t[0], px, fmaf(t[3], py, __fmul_rn(t[4], pz)));
     float vy = fmaf(t[3], px, fmaf(t[1], py, __fmul_rn(t[5], pz)));
     float vz = fmaf(t[4], px, fmaf(t[5], py, __fmul_rn(t[2], pz)));
-    vx = __fmul_rn(w, vx);
-    vy = __fmul_rn(w, vy);
-    vz = __fmul_rn(w, vz);
+    if (!W1) {
+        vx = __fmul_rn(w, vx);
+        vy = __fmul_rn(w, vy);
+        vz = __fmul_rn(w, vz);
+    }
     if (NN) {
         vx = __fsub_rn(vx, __fmul_rn(C, px));
         vy = __fsub_rn(vy, __fmul_rn(C, py));
@@ -515,8 +520,13 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                     atomicAdd(tile + cs + sm, (int)(ny - oy));
                     atomicAdd(tile + 2 * cs + sm, (int)(nz - oz));
                 } else {
-                    q_contrib(Tq[k], nnp[k], L2, C, gscale, en.y, en.z, en.w, nx, ny, nz);
-                    q_contrib(Tq[k], nnp[k], L2, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
+                    if (L2 == 1.0f) {
+                        q_contrib<true>(Tq[k], nnp[k], L2, C, gscale, en.y, en.z, en.w, nx, ny, nz);
+                        q_contrib<true>(Tq[k], nnp[k], L2, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
+                    } else {
+                        q_contrib(Tq[k], nnp[k], L2, C, gscale, en.y, en.z, en.w, nx, ny, nz);
+                        q_contrib(Tq[k], nnp[k], L2, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
+                    }
                     const int ix = (int)(nx - ox), iy = (int)(ny - oy), iz = (int)(nz - oz);
                     atomicAdd(tile + sp, ix);
                     atomicAdd(tile + cs + sp, iy);

@@ -16,7 +16,7 @@ the reference itself are what pin the CPU oracle:
                         T in {500,700,1000}; cutoff 3 / 30 % vacancies /
                         Efield (0,0,0.1) at T in {150,300}; cutoff 4 /
                         CageStrain 0.5 / Efield (0.05,0,0.05) / 10 % vacancies
-                        at T in {200,300}; 200 production sweeps after a
+                        at T in {300,500}; 200 production sweeps after a
                         per-temperature equilibration
   ref_analysis.npz      dipole_potential, dipole_electricfield(4),
                         dipole_electricfieldoffset(2) maps, polarisation(),
@@ -65,15 +65,16 @@ TRAJ_CASES = [
 # ~0.01 per 100 sweeps after 3000 sweeps at 300 K), so it has no equilibrium
 # to compare within any affordable run and is sampled at 500-1000 K; the
 # vacancy lattice at 150 K settles after about 2000 sweeps; the cutoff-4
-# lattice still drifts after 2500 sweeps at 150 K and is sampled at 200 K
-# after 3000.  The test checks that every series it compares is stationary.
+# lattice keeps relaxing for tens of thousands of sweeps at 200 K (both the
+# reference and the GPU sweeps, measured) and is sampled at 300 and 500 K.
+# The test checks that every series it compares is stationary.
 EQ_CASES = [
     dict(name="plain", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.0), occupancy=1.0, T=(500, 700, 1000),
          equil=(500, 500, 500)),
     dict(name="vacfield", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.1), occupancy=0.7, T=(150, 300),
          equil=(2500, 500)),
-    dict(name="rc4cage", L=32, cutoff=4, cage_strain=0.5, efield=(0.05, 0.0, 0.05), occupancy=0.9, T=(200, 300),
-         equil=(3000, 500)),
+    dict(name="rc4cage", L=32, cutoff=4, cage_strain=0.5, efield=(0.05, 0.0, 0.05), occupancy=0.9, T=(300, 500),
+         equil=(500, 500)),
 ]
 EQ_SEEDS = 16
 EQ_PROD = 200

@@ -14,7 +14,8 @@ sweeps (tests/golden/make_golden.py), for three Hamiltonians:
             (0, 0, 0.1) (src/starrynight-montecarlo-core.c:120-121), T in
             {150, 300} K;
   rc4cage   cutoff 4, CageStrain 0.5, Efield (0.05, 0, 0.05), 10 % vacancies,
-            T in {200, 300} K.
+            T in {300, 500} K (at 200 K it keeps relaxing for more than
+            10^4 sweeps on both sides: no equilibrium within reach).
 The colour sweep satisfies detailed balance with the same stationary
 distribution, so equilibrium averages -- not trajectories -- must agree, and
 only where both sides are in equilibrium: every compared series must be
