@@ -14,8 +14,9 @@
 //
 // Fixed point, exactly.  Each neighbour's contribution is rounded to a
 // fixed-point grid of 2^-k on its own, Q(c_ij) with c_ij = w (T_o p_j) -
-// CageStrain [|o| = 1] p_j, w = len_i len_j, and g_i is the int32 sum of
-// those integers.  A move of site a from p to p' then changes g_n by exactly
+// CageStrain [|o| = 1] p_j, w = len_i len_j (for unit uniform lengths
+// c_ij = (T_o - CageStrain [|o| = 1] I) p_j, the cage strain folded into the
+// tensor), and g_i is the int32 sum of those integers.  A move of site a from p to p' then changes g_n by exactly
 // Q(c(p')) - Q(c(p)), which the sweep adds with integer atomics: integer
 // addition is associative, so g after any sequence of moves equals, bit for
 // bit, the g that the field pass (gfield_tiled) computes from scratch for
@@ -85,7 +86,10 @@ __device__ __forceinline__ uint32_t q_bits(float v, float scale) { return __floa
 // Every kernel that builds or updates the field cache calls this function, so
 // the rounding is the same everywhere.
 // W1: w is known to be 1 (uniform lengths of 1), and the multiplication by it,
-// which is exact, is skipped.
+// which is exact, is skipped.  For w = 1 the cage-strain term is folded into
+// the tensor instead (the callers pass t with its diagonal reduced by C,
+// rounded once, and NN = false): c = (T - C I) p for |o| = 1.  The field-cache
+// pass folds the same way, so both compute the same floats.
 template <bool W1 = false>
 __device__ __forceinline__ void q_contrib(const float (&t)[6], bool NN, float w, float C, float scale, float px,
                                           float py, float pz, uint32_t &qx, uint32_t &qy, uint32_t &qz)
@@ -439,6 +443,12 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                     nnp[k] = P.nn != 0;
 #pragma unroll
                     for (int e = 0; e < 6; e++) Tq[k][e] = P.t[e];
+                    if (!MIXED && L2 == 1.0f && nnp[k]) {  // unit lengths: cage strain folded into the tensor
+                        Tq[k][0] = __fsub_rn(Tq[k][0], C);
+                        Tq[k][1] = __fsub_rn(Tq[k][1], C);
+                        Tq[k][2] = __fsub_rn(Tq[k][2], C);
+                        nnp[k] = false;
+                    }
                 }
             }
             gchunk = g;
@@ -642,6 +652,10 @@ __device__ __forceinline__ void q_pair(const float *__restrict__ tp, int cs, int
     constexpr float t5 = (float)sn_stencil::tensor_d(o.x, o.y, o.z, 5);
     constexpr bool NN = o.x * o.x + o.y * o.y + o.z * o.z == 1;
     const int d = (o.x * T1 + o.y) * T2 + o.z;
+    // unit uniform lengths: the cage strain folded into the diagonal (as the sweep's scatter does)
+    const bool fold = NN && !MIXED && w_u == 1.0f;
+    const float m0 = fold ? __fsub_rn(t0, C) : t0, m1 = fold ? __fsub_rn(t1, C) : t1,
+                m2 = fold ? __fsub_rn(t2, C) : t2;
 #pragma unroll
     for (int side = 0; side < 2; side++) {
         const int sj = side ? slot - d : slot + d;
@@ -650,11 +664,11 @@ __device__ __forceinline__ void q_pair(const float *__restrict__ tp, int cs, int
         // vx = fmaf(t0, px, fmaf(t3, py, t4 * pz)) and so on, without the zero terms
         float vx = t4 != 0.0f ? __fmul_rn(t4, pz) : 0.0f;
         if (t3 != 0.0f) vx = fmaf(t3, py, vx);
-        vx = fmaf(t0, px, vx);
+        vx = fmaf(m0, px, vx);
         float vy = t5 != 0.0f ? __fmul_rn(t5, pz) : 0.0f;
-        vy = fmaf(t1, py, vy);
+        vy = fmaf(m1, py, vy);
         if (t3 != 0.0f) vy = fmaf(t3, px, vy);
-        float vz = __fmul_rn(t2, pz);
+        float vz = __fmul_rn(m2, pz);
         if (t5 != 0.0f) vz = fmaf(t5, py, vz);
         if (t4 != 0.0f) vz = fmaf(t4, px, vz);
         if (MIXED || w != 1.0f) {
@@ -662,7 +676,7 @@ __device__ __forceinline__ void q_pair(const float *__restrict__ tp, int cs, int
             vy = __fmul_rn(w, vy);
             vz = __fmul_rn(w, vz);
         }
-        if (NN) {
+        if (NN && !fold) {
             vx = __fsub_rn(vx, __fmul_rn(C, px));
             vy = __fsub_rn(vy, __fmul_rn(C, py));
             vz = __fsub_rn(vz, __fmul_rn(C, pz));
