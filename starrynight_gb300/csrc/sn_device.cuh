@@ -67,11 +67,13 @@ __device__ __forceinline__ bool sn_try_point(uint32_t ra, uint32_t rb, int dim, 
     return true;
 }
 
-// Returns false when every try was rejected (the move then keeps the old dipole).
-__device__ __forceinline__ bool sn_proposal(uint32_t site, uint32_t sweep, uint32_t stream, uint2 key,
-                                            int dim, int constrain, float3 &p, float &u)
+// Draw 0 of a proposal: the accept uniform u, and the first try (or the axis
+// for ConstrainToX).  False when the try was rejected: sn_proposal_retry then
+// continues with draws 1, 2, ...
+__device__ __forceinline__ bool sn_proposal_first(uint32_t site, uint32_t sweep, uint32_t stream, uint2 key,
+                                                  int dim, int constrain, float3 &p, float &u)
 {
-    uint4 r = sn_philox(make_uint4(site, sweep, 0u, stream), key);
+    const uint4 r = sn_philox(make_uint4(site, sweep, 0u, stream), key);
     u = sn_uniform24(r.x);
     if (constrain) {
         const uint32_t c = (uint32_t)(((uint64_t)r.w * 6ull) >> 32);
@@ -79,13 +81,26 @@ __device__ __forceinline__ bool sn_proposal(uint32_t site, uint32_t sweep, uint3
         p = make_float3(c >> 1 == 0 ? v : 0.0f, c >> 1 == 1 ? v : 0.0f, c >> 1 == 2 ? v : 0.0f);
         return true;
     }
-    if (sn_try_point(r.y, r.z, dim, p)) return true;
+    return sn_try_point(r.y, r.z, dim, p);
+}
+
+__device__ __forceinline__ bool sn_proposal_retry(uint32_t site, uint32_t sweep, uint32_t stream, uint2 key,
+                                                  int dim, float3 &p)
+{
     for (uint32_t k = 1; k < SN_PROPOSAL_MAX_DRAWS; k++) {
-        r = sn_philox(make_uint4(site, sweep, k, stream), key);
+        const uint4 r = sn_philox(make_uint4(site, sweep, k, stream), key);
         if (sn_try_point(r.x, r.y, dim, p)) return true;
         if (sn_try_point(r.z, r.w, dim, p)) return true;
     }
     return false;
+}
+
+// Returns false when every try was rejected (the move then keeps the old dipole).
+__device__ __forceinline__ bool sn_proposal(uint32_t site, uint32_t sweep, uint32_t stream, uint2 key,
+                                            int dim, int constrain, float3 &p, float &u)
+{
+    return sn_proposal_first(site, sweep, stream, key, dim, constrain, p, u) ||
+           sn_proposal_retry(site, sweep, stream, key, dim, p);
 }
 
 // ---------------------------------------------------------------------------

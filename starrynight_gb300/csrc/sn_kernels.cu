@@ -218,26 +218,96 @@ __global__ void proposal_batch_kernel(const uint32_t *site, uint32_t sweep, uint
 // here with full parallelism instead of inside the sweep's block schedule.
 // Thresholds are -ln(u)/beta (accept iff dE < threshold); vacancies get -1.
 // A proposal whose Marsaglia tries all fail keeps the old dipole.
-__global__ void sweep_proposals_kernel(const SnReplicaDev *reps, const uint32_t *sweep_ctr, int dim, int constrain)
+//
+// Lanes are kept busy by compaction: a warp takes a chunk of 256 sites,
+// writes the vacancies at once and queues the occupied sites (warp ballot),
+// draws the first try for 32 queued sites at a time, and queues the ~21 % of
+// sites whose first try was rejected; those are redrawn 32 at a time, the
+// remainder carried to the warp's next chunk.  Without it a warp pays for
+// its vacant lanes and runs a second draw whenever any one lane needs it,
+// which is almost always.
+#define SN_PROP_CHUNK 256
+#define SN_PROP_WARPS 8
+
+__device__ __forceinline__ void proposal_retry_out(const SnReplicaDev &R, float4 *out, uint32_t site, float thr,
+                                                   uint32_t sweep, uint2 key, int dim)
 {
+    float3 p;
+    if (!sn_proposal_retry(site, sweep, SN_STREAM_SWEEP, key, dim, p))
+        p = make_float3(R.px[site], R.py[site], R.pz[site]);
+    out[site] = make_float4(p.x, p.y, p.z, thr);
+}
+
+__global__ void __launch_bounds__(SN_PROP_WARPS * 32)
+    sweep_proposals_kernel(const SnReplicaDev *reps, const uint32_t *sweep_ctr, int dim, int constrain)
+{
+    __shared__ uint32_t qsite[SN_PROP_WARPS][SN_PROP_CHUNK];
+    __shared__ uint32_t fsite[SN_PROP_WARPS][SN_PROP_CHUNK + 32];
+    __shared__ float fthr[SN_PROP_WARPS][SN_PROP_CHUNK + 32];
     const SnReplicaDev &R = reps[blockIdx.y];
     float4 *out = R.prop;
     if (!out) return;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
     const uint32_t sweep = *sweep_ctr;
     const uint2 key = make_uint2(R.seed_lo, R.seed_hi);
     const float beta = R.beta;
     const long long n = R.n_sites;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        float4 pr = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-        if (R.len[i] != 0.0f) {
-            float3 p;
-            float u;
-            if (!sn_proposal((uint32_t)i, sweep, SN_STREAM_SWEEP, key, dim, constrain, p, u))
-                p = make_float3(R.px[i], R.py[i], R.pz[i]);
-            pr = make_float4(p.x, p.y, p.z, u > 0.0f ? -logf(u) / beta : INFINITY);
+    const float *__restrict__ len = R.len;
+    uint32_t *q = qsite[wib], *fs = fsite[wib];
+    float *ft = fthr[wib];
+    int nf = 0;  // rejected first tries queued in fs/ft (warp-uniform)
+    const long long stride = (long long)gridDim.x * SN_PROP_WARPS * SN_PROP_CHUNK;
+    for (long long c0 = ((long long)blockIdx.x * SN_PROP_WARPS + wib) * SN_PROP_CHUNK; c0 < n; c0 += stride) {
+        // 1. occupied sites of the chunk into q, in site order; vacancies written here
+        float lv[SN_PROP_CHUNK / 32];
+#pragma unroll
+        for (int j = 0; j < SN_PROP_CHUNK / 32; j++) {
+            const long long i = c0 + 32 * j + lane;
+            lv[j] = i < n ? __ldg(len + i) : 0.0f;
         }
-        out[i] = pr;
+        int nq = 0;
+#pragma unroll
+        for (int j = 0; j < SN_PROP_CHUNK / 32; j++) {
+            const long long i = c0 + 32 * j + lane;
+            const bool occ = lv[j] != 0.0f;
+            if (i < n && !occ) out[i] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+            const unsigned m = __ballot_sync(0xffffffffu, occ);
+            if (occ) q[nq + __popc(m & below)] = (uint32_t)i;
+            nq += __popc(m);
+        }
+        __syncwarp();
+        // 2. draw 0 for the queued sites, 32 at a time; rejected tries to fs/ft
+        for (int b = 0; b < nq; b += 32) {
+            bool rej = false;
+            uint32_t site = 0;
+            float thr = 0.0f;
+            if (b + lane < nq) {
+                site = q[b + lane];
+                float3 p;
+                float u;
+                const bool ok = sn_proposal_first(site, sweep, SN_STREAM_SWEEP, key, dim, constrain, p, u);
+                thr = u > 0.0f ? -logf(u) / beta : INFINITY;
+                if (ok) out[site] = make_float4(p.x, p.y, p.z, thr);
+                rej = !ok;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, rej);
+            if (rej) {
+                const int e = nf + __popc(m & below);
+                fs[e] = site;
+                ft[e] = thr;
+            }
+            nf += __popc(m);
+        }
+        __syncwarp();
+        // 3. full rounds of retries
+        while (nf >= 32) {
+            nf -= 32;
+            proposal_retry_out(R, out, fs[nf + lane], ft[nf + lane], sweep, key, dim);
+            __syncwarp();
+        }
     }
+    if (lane < nf) proposal_retry_out(R, out, fs[lane], ft[lane], sweep, key, dim);
 }
 
 // FP32 FMA throughput probe: 8 independent chains per thread, no memory
@@ -360,6 +430,6 @@ cudaError_t sn_launch_sweep_proposals(const SnReplicaDev *reps, int nrep, const 
 {
     if (nrep <= 0) return cudaSuccess;
     const int bx = std::max(1, (4 * sms + nrep - 1) / nrep);
-    sweep_proposals_kernel<<<dim3(bx, nrep), 256, 0, st>>>(reps, sweep, dim, constrain);
+    sweep_proposals_kernel<<<dim3(bx, nrep), SN_PROP_WARPS * 32, 0, st>>>(reps, sweep, dim, constrain);
     return cudaGetLastError();
 }

@@ -56,9 +56,11 @@ __host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, 
     c.props = o;
     o += (uint32_t)(2 * pc * tg) * 32u;  // two chunks of (p', threshold), (p_old, -) per target
     c.list = o;
-    o += (uint32_t)tg * 32u;         // accepted moves of a group
+    o += (uint32_t)((tg + 31) / 32) * 32u * 32u;  // accepted moves of a group: 32 entries per target warp
     c.cnt = o;
-    o += 32u;  // two group counters, the tile-copy mbarrier (bytes 8..15), its phase parity
+    // the tile-copy mbarrier (bytes 8..15), its phase parity (16..19), the
+    // target warps' accepted-move counts (32..63)
+    o += 64u;
     c.red = o;
     o += (SN_CACHED_THREADS / 32) * 16u * 8u;
     c.total = o;
@@ -353,7 +355,8 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         move_tile<false>(R, Gm, w, tile, tlen, tid, NT);
     }
     cp_async_commit();
-    if (tid < 2) cnt[tid] = 0;
+    int *wc = cnt + 8;  // accepted moves per target warp in the current group
+    const int nAw = (tg + 31) >> 5;  // target warps
 
     // this thread's target role: target tt of every colour group.  All
     // threads stage proposals (thread tid for target tt = tid % tg of groups
@@ -456,61 +459,68 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         }
 
         // ---- A. targets of the group: dE from the cached field, accept, record ---------
-        bool acc = false;
-        float dx = 0.0f, dy = 0.0f, dz = 0.0f, Li = Lu;
-        int tslot = 0;
-        if (tid < tg) {
-            int cx, cy, cz;
-            group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
-            const float4 pr = cur[2 * ((g - gchunk) * tg + tt)];
-            if (pr.w >= 0.0f) {
-                const float4 po = cur[2 * ((g - gchunk) * tg + tt) + 1];
+        // Warp w lists its accepted moves in entries 32 w ... of the group's
+        // list and their number in wc[w] (no shared counter to contend for).
+        if (warp < nAw) {
+            bool acc = false;
+            float dx = 0.0f, dy = 0.0f, dz = 0.0f, Li = Lu;
+            int tslot = 0;
+            float4 pr = make_float4(0.0f, 0.0f, 0.0f, -2.0f), po = pr;
+            if (tid < tg) {
+                int cx, cy, cz;
+                group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
+                pr = cur[2 * ((g - gchunk) * tg + tt)];
+                po = cur[2 * ((g - gchunk) * tg + tt) + 1];
                 tslot = ((cx + Gm.cH[0]) * T1 + (cy + Gm.cH[1])) * T2 + cz + Gm.cH[2] + trel;
-                const float gx = fmaf((float)tile[tslot], ginv, Ex);
-                const float gy = fmaf((float)tile[cs + tslot], ginv, Ey);
-                const float gz = fmaf((float)tile[2 * cs + tslot], ginv, Ez);
-                dx = pr.x - po.x;
-                dy = pr.y - po.y;
-                dz = pr.z - po.z;
-                float dE = fmaf(dx, gx, fmaf(dy, gy, dz * gz));
-                if (Kk > 0.0f) dE -= Kk * ((fabsf(pr.x) - fabsf(po.x)) + (fabsf(pr.y) - fabsf(po.y)));
-                satt++;
-                if (dE < pr.w) {
-                    acc = true;
-                    const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
-                    gpx[site] = pr.x;
-                    gpy[site] = pr.y;
-                    gpz[site] = pr.z;
-                    if (MIXED) Li = tlen[tslot];
-                    sacc++;
-                    sdE.add(dE);
-                    sPx.add(Li * dx);
-                    sPy.add(Li * dy);
-                    sPz.add(Li * dz);
+                if (pr.w >= 0.0f) {
+                    const float gx = fmaf((float)tile[tslot], ginv, Ex);
+                    const float gy = fmaf((float)tile[cs + tslot], ginv, Ey);
+                    const float gz = fmaf((float)tile[2 * cs + tslot], ginv, Ez);
+                    dx = pr.x - po.x;
+                    dy = pr.y - po.y;
+                    dz = pr.z - po.z;
+                    float dE = fmaf(dx, gx, fmaf(dy, gy, dz * gz));
+                    if (Kk > 0.0f) dE -= Kk * ((fabsf(pr.x) - fabsf(po.x)) + (fabsf(pr.y) - fabsf(po.y)));
+                    satt++;
+                    if (dE < pr.w) {
+                        acc = true;
+                        const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
+                        gpx[site] = pr.x;
+                        gpy[site] = pr.y;
+                        gpz[site] = pr.z;
+                        if (MIXED) Li = tlen[tslot];
+                        sacc++;
+                        sdE.add(dE);
+                        sPx.add(Li * dx);
+                        sPy.add(Li * dy);
+                        sPz.add(Li * dz);
+                    }
                 }
             }
-            // accepted moves of the warp go to the group's list at a base taken atomically
             // (the list order does not matter: the scatter adds integers)
             const unsigned m = __ballot_sync(0xffffffffu, acc);
-            int base = 0;
-            if (lane == 0 && m) base = atomicAdd(&cnt[g & 1], __popc(m));
-            base = __shfl_sync(0xffffffffu, base, 0);
             if (acc) {
-                const int e = base + __popc(m & ((1u << lane) - 1u));
-                const float4 pr = cur[2 * ((g - gchunk) * tg + tt)];
-                const float4 po = cur[2 * ((g - gchunk) * tg + tt) + 1];
+                const int e = 32 * warp + __popc(m & ((1u << lane) - 1u));
                 list[2 * e] = make_float4(__int_as_float(tslot), pr.x, pr.y, pr.z);
                 list[2 * e + 1] = make_float4(po.x, po.y, po.z, Li);
             }
+            if (lane == 0) wc[warp] = __popc(m);
         }
-        if (tid == NT - 1) cnt[(g + 1) & 1] = 0;  // the next group's counter (last read a group ago)
         __syncthreads();
 
         // ---- B. scatter the accepted moves' field changes into the tile --------------
-        // dg_n = Q(c(p')) - Q(c(p)) for n = a +- o (the magic bias cancels)
-        const int n = cnt[g & 1];
+        // dg_n = Q(c(p')) - Q(c(p)) for n = a +- o (the magic bias cancels).
+        // Moves e = pj, pj + GRP, ... of the warps' lists taken in warp order.
+        int n = wc[0];
+        for (int q = 1; q < nAw; q++) n += wc[q];
+        int lw = 0, lbase = 0, lcnt = wc[0];  // list region of the current move
         for (int e = pj; e < n && prole; e += GRP) {
-            const float4 en = list[2 * e], eo = list[2 * e + 1];
+            while (e - lbase >= lcnt) {
+                lbase += lcnt;
+                lcnt = wc[++lw];
+            }
+            const int le = 32 * lw + e - lbase;
+            const float4 en = list[2 * le], eo = list[2 * le + 1];
             const int sa = __float_as_int(en.x);
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
