@@ -27,11 +27,14 @@
 //
 // Ownership.  A block's tile is the block plus a halo of `cutoff` sites
 // (the z halo rounded up to 4 sites for 16-byte rows).  It is loaded when the
-// block starts and the WHOLE tile is stored back when the block ends: with
-// every block side >= 2 cutoff (a planner condition), tiles of blocks that
-// can run at the same time (not adjacent) are disjoint, and adjacent blocks
-// run one after the other (block colours; the dataflow kernel's dependency
-// waits), so each site's g is held by at most one running block.
+// block starts and stored back when the block ends: with every block side
+// >= 2 cutoff (a planner condition), the cutoff-wide parts of the tiles of
+// blocks that can run at the same time (not adjacent) are disjoint, and
+// adjacent blocks run one after the other (block colours; the dataflow
+// kernel's dependency waits), so each site's g is held by at most one
+// running block.  The store covers the cutoff-wide tile, or the whole tile
+// when the z side is at least twice the rounded z halo (whole tiles are then
+// disjoint too).
 #pragma once
 
 namespace sn_sweep {
@@ -296,11 +299,22 @@ __device__ __forceinline__ void move_tile(const SnReplicaDev &R, const SnTile &G
     }
 }
 
+// Move statistic k (0: sum dE, 1-3: sum dP, 4: accepted, 5: attempted) of
+// some blocks into a replica's per-sweep totals.
+__device__ __forceinline__ void sn_add_move_stats(SnAccum *A, int k, double v)
+{
+    if (k == 0) atomicAdd(&A->dE, v);
+    else if (k < 4) atomicAdd(&A->dP[k - 1], v);
+    else if (k == 4) atomicAdd(&A->acc, (unsigned long long)v);
+    else atomicAdd(&A->att, (unsigned long long)v);
+}
+
 // fill: write the stencil pair table into shared memory (once per CTA: the
-// table depends on the cutoff only).
+// table depends on the cutoff only).  cta_acc: the CTA's running move
+// statistics for this block's replica (nullptr: add to the replica's totals).
 template <int RC, bool MIXED, bool FLOW>
 __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhaseArgs &a, unsigned char *smem,
-                                                   bool fill)
+                                                   bool fill, double *cta_acc)
 {
     using G = Geo<RC, false>;
     constexpr int S = G::S, NP = G::NP;
@@ -561,7 +575,10 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     }
 
     // ---- the tile's fields back to HBM ---------------------------------------------
-    move_tile<true>(R, Gm, w, tile, nullptr, tid, NT, RC);
+    // (the whole rounded z halo when z blocks are at least twice as long as
+    // it: tiles of blocks that may run together are then disjoint with it,
+    // and every row is written in whole 16-byte chunks)
+    move_tile<true>(R, Gm, w, tile, nullptr, tid, NT, Bz >= 2 * Gm.cH[2] ? Gm.cH[2] : RC);
 
     // ---- the block's final sites to the caller's buffer ---------------------------
     if (float *out = R.out_xyz) {
@@ -609,11 +626,8 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     if (tid < 6) {
         double s = 0.0;
         for (int q = 0; q < (NT >> 5); q++) s += red[q * 16 + tid];
-        SnAccum *A = a.acc + w.rep;
-        if (tid == 0) atomicAdd(&A->dE, s);
-        else if (tid < 4) atomicAdd(&A->dP[tid - 1], s);
-        else if (tid == 4) atomicAdd(&A->acc, (unsigned long long)s);
-        else atomicAdd(&A->att, (unsigned long long)s);
+        if (cta_acc) cta_acc[tid] += s;
+        else sn_add_move_stats(a.acc + w.rep, tid, s);
     }
 }
 
