@@ -552,9 +552,9 @@ struct SweepBounds {
 
 template <int RC, bool TWO_D, bool MIXED, bool CACHED, bool FLOW>
 __device__ __forceinline__ void sweep_block_any(const SnWork w, const SnPhaseArgs &a, unsigned char *smem, bool first,
-                                                double *cta_acc = nullptr)
+                                                CStats *cst = nullptr)
 {
-    if constexpr (CACHED && !TWO_D) sweep_block_cached<RC, MIXED, FLOW>(w, a, smem, first, cta_acc);
+    if constexpr (CACHED && !TWO_D) sweep_block_cached<RC, MIXED, FLOW>(w, a, smem, first, cst);
     else sweep_block<RC, TWO_D, MIXED, FLOW>(w, a, smem);
 }
 
@@ -595,22 +595,19 @@ __global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACH
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_item;
-    // cached sweep: the move statistics of this CTA's blocks of replica
-    // s_rep, added to the replica's totals when the replica changes and at
-    // the end (instead of global FP64 atomics on every block)
-    __shared__ double s_acc[6];
-    __shared__ int s_rep;
+    // cached sweep: each thread's move statistics over the CTA's blocks of
+    // replica cur_rep, added to the replica's totals when the replica changes
+    // and at the end (not reduced and added on every block)
+    CStats st;
+    int cur_rep = -1;
     const int tid = threadIdx.x;
     const uint32_t epoch = *f.base.sweep + 1u;
     bool first = true;  // this CTA's first block (per-CTA shared-memory tables)
-    if (tid == 0) {
-        s_item = (int)atomicAdd(f.queue, 1u);
-        s_rep = -1;
-    }
+    if (tid == 0) s_item = (int)atomicAdd(f.queue, 1u);
     __syncthreads();
     int item = s_item;
     for (;;) {
-        __syncthreads();  // every thread has read s_item and s_rep
+        __syncthreads();  // every thread has read s_item
         if (item >= f.base.n_work) break;
         // the next block is taken now, so the queue's latency overlaps this
         // block (no deadlock: the earliest unfinished block in queue order
@@ -633,22 +630,16 @@ __global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACH
                 atomicAdd(f.err + 2, (unsigned)it);
             }
         }
-        double *cacc = nullptr;
         if constexpr (CACHED && !TWO_D) {
-            const int rep = f.base.work[item].rep;
-            if (rep != s_rep) {
-                if (tid < 6) {
-                    if (s_rep >= 0) sn_add_move_stats(f.base.acc + s_rep, tid, s_acc[tid]);
-                    s_acc[tid] = 0.0;
-                }
+            const int rep = f.base.work[item].rep;  // the same for every thread
+            if (rep != cur_rep) {
+                if (cur_rep >= 0) flush_cstats(st, reinterpret_cast<double *>(smem), f.base.acc + cur_rep);
+                cur_rep = rep;
             }
-            cacc = s_acc;
-            __syncthreads();
-            if (tid == 0) s_rep = rep;
         }
         __syncthreads();
         __threadfence();
-        sweep_block_any<RC, TWO_D, MIXED, CACHED, true>(f.base.work[item], f.base, smem, first, cacc);
+        sweep_block_any<RC, TWO_D, MIXED, CACHED, true>(f.base.work[item], f.base, smem, first, &st);
         first = false;
         __syncthreads();
         if (tid == 0) {
@@ -658,7 +649,7 @@ __global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACH
         item = s_item;
     }
     if constexpr (CACHED && !TWO_D) {
-        if (tid < 6 && s_rep >= 0) sn_add_move_stats(f.base.acc + s_rep, tid, s_acc[tid]);
+        if (cur_rep >= 0) flush_cstats(st, reinterpret_cast<double *>(smem), f.base.acc + cur_rep);
     }
 }
 

@@ -48,8 +48,11 @@ __host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, 
 {
     CCarve c;
     uint32_t o = 0;
-    // the pair table first: its place must not depend on the replica's tile,
-    // because a CTA fills it once for all the blocks it sweeps
+    // the reduction slots and the pair table first: their places must not
+    // depend on the replica's tile, because a CTA uses them across the blocks
+    // it sweeps (the move statistics are reduced when the replica changes)
+    c.red = o;
+    o += (SN_CACHED_THREADS / 32) * 16u * 8u;
     c.pairs = o;
     o += sn_align16((uint32_t)np * 48u);
     c.tile = o;
@@ -64,8 +67,6 @@ __host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, 
     // the tile-copy mbarrier (bytes 8..15), its phase parity (16..19), the
     // target warps' accepted-move counts (32..63)
     o += 64u;
-    c.red = o;
-    o += (SN_CACHED_THREADS / 32) * 16u * 8u;
     c.total = o;
     return c;
 }
@@ -299,22 +300,64 @@ __device__ __forceinline__ void move_tile(const SnReplicaDev &R, const SnTile &G
     }
 }
 
-// Move statistic k (0: sum dE, 1-3: sum dP, 4: accepted, 5: attempted) of
-// some blocks into a replica's per-sweep totals.
-__device__ __forceinline__ void sn_add_move_stats(SnAccum *A, int k, double v)
+// A thread's move statistics: compensated FP32 sums of dE and dP over its
+// accepted moves, and its accepted and attempted counts.
+struct CStats {
+    KahanF dE, Px, Py, Pz;
+    unsigned int acc = 0, att = 0;
+};
+
+// Adds every thread's statistics into the replica's per-sweep totals A and
+// clears them (all threads of the CTA call it; red: (NT / 32) * 16 doubles of
+// shared memory).  Within a warp the compensated FP32 sums are combined as
+// (sum, error) pairs by error-free additions (Knuth's TwoSum); FP64 (a slow
+// pipe on this GPU) is used only to add the warps' results.
+__device__ __forceinline__ void flush_cstats(CStats &st, double *red, SnAccum *A)
 {
-    if (k == 0) atomicAdd(&A->dE, v);
-    else if (k < 4) atomicAdd(&A->dP[k - 1], v);
-    else if (k == 4) atomicAdd(&A->acc, (unsigned long long)v);
-    else atomicAdd(&A->att, (unsigned long long)v);
+    constexpr int NT = SN_CACHED_THREADS;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float hs[4] = {st.dE.s, st.Px.s, st.Py.s, st.Pz.s}, hc[4] = {-st.dE.c, -st.Px.c, -st.Py.c, -st.Pz.c};
+    unsigned int ia = st.acc, it = st.att;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float bs = __shfl_xor_sync(0xffffffffu, hs[k], o), bc = __shfl_xor_sync(0xffffffffu, hc[k], o);
+            const float t2 = __fadd_rn(hs[k], bs);
+            const float bb = __fsub_rn(t2, hs[k]);
+            const float err = __fadd_rn(__fsub_rn(hs[k], __fsub_rn(t2, bb)), __fsub_rn(bs, bb));
+            hs[k] = t2;
+            hc[k] = __fadd_rn(__fadd_rn(hc[k], bc), err);
+        }
+        ia += __shfl_xor_sync(0xffffffffu, ia, o);
+        it += __shfl_xor_sync(0xffffffffu, it, o);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) red[warp * 16 + k] = (double)hs[k] + (double)hc[k];
+        red[warp * 16 + 4] = (double)ia;
+        red[warp * 16 + 5] = (double)it;
+    }
+    __syncthreads();
+    if (tid < 6) {
+        double v = 0.0;
+        for (int q = 0; q < (NT >> 5); q++) v += red[q * 16 + tid];
+        if (tid == 0) atomicAdd(&A->dE, v);
+        else if (tid < 4) atomicAdd(&A->dP[tid - 1], v);
+        else if (tid == 4) atomicAdd(&A->acc, (unsigned long long)v);
+        else atomicAdd(&A->att, (unsigned long long)v);
+    }
+    __syncthreads();  // red is free again
+    st = CStats();
 }
 
 // fill: write the stencil pair table into shared memory (once per CTA: the
-// table depends on the cutoff only).  cta_acc: the CTA's running move
-// statistics for this block's replica (nullptr: add to the replica's totals).
+// table depends on the cutoff only).  cst: the calling thread's running move
+// statistics for this block's replica, added up by the caller (nullptr: the
+// block adds its statistics to the replica's totals itself).
 template <int RC, bool MIXED, bool FLOW>
 __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhaseArgs &a, unsigned char *smem,
-                                                   bool fill, double *cta_acc)
+                                                   bool fill, CStats *cst)
 {
     using G = Geo<RC, false>;
     constexpr int S = G::S, NP = G::NP;
@@ -341,6 +384,8 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     const float Lu = R.length;
     const float gscale = R.gscale, ginv = R.ginv;  // 2^k, 2^-k
     const int cs = Gm.cslots;
+    const int cH0 = Gm.cH[0], cH1 = Gm.cH[1], cH2 = Gm.cH[2];
+    float4 *__restrict__ gprop = R.prop;
 
     const CCarve cv = sn_ccarve(cs, tg, pc, NP, MIXED);
     int *tile = reinterpret_cast<int *>(smem + cv.tile);
@@ -393,15 +438,21 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     int dq[PPT];
     bool nnp[PPT], qok[PPT];
 
-    KahanF sdE, sPx, sPy, sPz;
-    unsigned int sacc = 0, satt = 0;
+    CStats own;
+    CStats &st = cst ? *cst : own;
 
+    // amask bit g: this thread's target of group g exists (groups >= 64 are tested when staged).
+    // Block sides that are multiples of S give every colour the same count: all bits.
     unsigned long long amask = 0ull;
-    for (int g = 0; g < ng && g < 64; g++) {
-        int cx, cy, cz;
-        group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
-        if (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) && qz < sn_count(Bz, cz, S))
-            amask |= 1ull << g;
+    if (Bx % S == 0 && By % S == 0 && Bz % S == 0) {
+        if (tvalid) amask = ng >= 64 ? ~0ull : (1ull << ng) - 1ull;
+    } else {
+        for (int g = 0; g < ng && g < 64; g++) {
+            int cx, cy, cz;
+            group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
+            if (tvalid && qx < sn_count(Bx, cx, S) && qy < sn_count(By, cy, S) && qz < sn_count(Bz, cz, S))
+                amask |= 1ull << g;
+        }
     }
 
     // Proposals arrive in chunks of pc colour groups, copied asynchronously
@@ -423,7 +474,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                 float4 *slot = buf + 2 * (k * tg + tt);
                 if (tgt) {
                     const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
-                    cp_async16(slot, R.prop + site);
+                    cp_async16(slot, gprop + site);
                     cp_async4(&slot[1].x, gpx + site);
                     cp_async4(&slot[1].y, gpy + site);
                     cp_async4(&slot[1].z, gpz + site);
@@ -485,7 +536,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                 group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
                 pr = cur[2 * ((g - gchunk) * tg + tt)];
                 po = cur[2 * ((g - gchunk) * tg + tt) + 1];
-                tslot = ((cx + Gm.cH[0]) * T1 + (cy + Gm.cH[1])) * T2 + cz + Gm.cH[2] + trel;
+                tslot = ((cx + cH0) * T1 + (cy + cH1)) * T2 + cz + cH2 + trel;
                 if (pr.w >= 0.0f) {
                     const float gx = fmaf((float)tile[tslot], ginv, Ex);
                     const float gy = fmaf((float)tile[cs + tslot], ginv, Ey);
@@ -495,7 +546,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                     dz = pr.z - po.z;
                     float dE = fmaf(dx, gx, fmaf(dy, gy, dz * gz));
                     if (Kk > 0.0f) dE -= Kk * ((fabsf(pr.x) - fabsf(po.x)) + (fabsf(pr.y) - fabsf(po.y)));
-                    satt++;
+                    st.att++;
                     if (dE < pr.w) {
                         acc = true;
                         const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
@@ -503,11 +554,11 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                         gpy[site] = pr.y;
                         gpz[site] = pr.z;
                         if (MIXED) Li = tlen[tslot];
-                        sacc++;
-                        sdE.add(dE);
-                        sPx.add(Li * dx);
-                        sPy.add(Li * dy);
-                        sPz.add(Li * dz);
+                        st.acc++;
+                        st.dE.add(dE);
+                        st.Px.add(Li * dx);
+                        st.Py.add(Li * dy);
+                        st.Pz.add(Li * dz);
                     }
                 }
             }
@@ -595,40 +646,8 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         }
     }
 
-    // ---- block reduction of the move statistics ---------------------------------
-    // Within a warp the compensated FP32 sums are combined as (sum, error)
-    // pairs by error-free additions (Knuth's TwoSum); FP64 (a slow pipe on this
-    // GPU) is used only to add the warps' results.
-    float hs[4] = {sdE.s, sPx.s, sPy.s, sPz.s}, hc[4] = {-sdE.c, -sPx.c, -sPy.c, -sPz.c};
-    unsigned int ia = sacc, it = satt;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const float bs = __shfl_xor_sync(0xffffffffu, hs[k], o), bc = __shfl_xor_sync(0xffffffffu, hc[k], o);
-            const float t2 = __fadd_rn(hs[k], bs);
-            const float bb = __fsub_rn(t2, hs[k]);
-            const float err = __fadd_rn(__fsub_rn(hs[k], __fsub_rn(t2, bb)), __fsub_rn(bs, bb));
-            hs[k] = t2;
-            hc[k] = __fadd_rn(__fadd_rn(hc[k], bc), err);
-        }
-        ia += __shfl_xor_sync(0xffffffffu, ia, o);
-        it += __shfl_xor_sync(0xffffffffu, it, o);
-    }
-    if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < 4; k++) red[warp * 16 + k] = (double)hs[k] + (double)hc[k];
-        red[warp * 16 + 4] = (double)ia;
-        red[warp * 16 + 5] = (double)it;
-    }
-    __syncthreads();
     if (a.tile_copy && tid == 0) cnt[4] = (int)(tphase ^ 1u);  // read by the CTA's next block after its barriers
-    if (tid < 6) {
-        double s = 0.0;
-        for (int q = 0; q < (NT >> 5); q++) s += red[q * 16 + tid];
-        if (cta_acc) cta_acc[tid] += s;
-        else sn_add_move_stats(a.acc + w.rep, tid, s);
-    }
+    if (!cst) flush_cstats(own, red, a.acc + w.rep);
 }
 
 // ---------------------------------------------------------------------------
