@@ -238,7 +238,7 @@ __device__ __forceinline__ void proposal_retry_out(const SnReplicaDev &R, float4
     out[site] = make_float4(p.x, p.y, p.z, thr);
 }
 
-__global__ void __launch_bounds__(SN_PROP_WARPS * 32)
+__global__ void __launch_bounds__(SN_PROP_WARPS * 32, 4)
     sweep_proposals_kernel(const SnReplicaDev *reps, const uint32_t *sweep_ctr, int dim, int constrain)
 {
     __shared__ uint32_t qsite[SN_PROP_WARPS][SN_PROP_CHUNK];
@@ -429,7 +429,20 @@ cudaError_t sn_launch_sweep_proposals(const SnReplicaDev *reps, int nrep, const 
                                       int constrain, int sms, cudaStream_t st)
 {
     if (nrep <= 0) return cudaSuccess;
-    const int bx = std::max(1, (4 * sms + nrep - 1) / nrep);
+    // one wave of resident blocks (the blocks stride over the sites); the
+    // occupancy is looked up once per device
+    static int per_sm_dev[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    int per_sm = per_sm_dev[dev];
+    if (per_sm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_proposals_kernel, SN_PROP_WARPS * 32, 0) !=
+                cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        per_sm_dev[dev] = per_sm;
+    }
+    const int bx = std::max(1, per_sm * sms / nrep);
     sweep_proposals_kernel<<<dim3(bx, nrep), SN_PROP_WARPS * 32, 0, st>>>(reps, sweep, dim, constrain);
     return cudaGetLastError();
 }
