@@ -11,10 +11,10 @@ the reference itself are what pin the CPU oracle:
                         with ACCEPT/REJECT, for several parameter sets
   ref_site_energy.npz   site_energy() values for random trial moves
   ref_equilibrium.npz   per-sweep E/site and |P|/site of random-sequential runs
-                        (statistical oracle), 16 seeds per temperature, 32^3:
+                        (statistical oracle), 32 seeds per temperature, 32^3:
                         cutoff 3 / CageStrain 1 / no field / all occupied at
                         T in {500,700,1000}; cutoff 3 / 30 % vacancies /
-                        Efield (0,0,0.1) at T in {150,300}; cutoff 4 /
+                        Efield (0,0,0.1) at T in {300,500}; cutoff 4 /
                         CageStrain 0.5 / Efield (0.05,0,0.05) / 10 % vacancies
                         at T in {300,500}; 200 production sweeps after a
                         per-temperature equilibration
@@ -55,28 +55,31 @@ TRAJ_CASES = [
          prevalence=(0.5, 0.3, 0.2), efield=(0.0, 0.0, 0.2), moves=8000),
 ]
 
-# Statistical oracle: three Hamiltonians, 16 independent reference runs per
+# Statistical oracle: three Hamiltonians, 32 independent reference runs per
 # temperature.  "plain" is the small cubic case (all sites occupied, no field);
 # "vacfield" the solid solution with vacancies zeroed after solid_solution and
 # a field along z (the physics of the 256^3 benchmark lattice); "rc4cage"
 # cutoff 4 with a weaker cage strain, an oblique field and 10 % vacancies.
-# Equilibration lengths come from long single reference runs: below 500 K the
-# plain lattice keeps ordering slowly (its energy per site still falls by
-# ~0.01 per 100 sweeps after 3000 sweeps at 300 K), so it has no equilibrium
-# to compare within any affordable run and is sampled at 500-1000 K; the
-# vacancy lattice at 150 K settles after about 2000 sweeps; the cutoff-4
-# lattice keeps relaxing for tens of thousands of sweeps at 200 K (both the
-# reference and the GPU sweeps, measured) and is sampled at 300 and 500 K.
-# The test checks that every series it compares is stationary.
+# Temperatures and equilibration lengths come from relaxation curves measured
+# on both sides (reference runs on the CPU, 32 GPU replicas up to 20000
+# sweeps): at these temperatures E/site is flat after a few hundred sweeps,
+# except for cutoff 4 at 300 K, where the reference's random-sequential
+# moves still lower E/site by a few 10^-3 between 500 and 1500 sweeps (the
+# colour sweep is flat from about 1000): its runs equilibrate for 3000.
+# Below these temperatures the lattices keep ordering for thousands (plain
+# lattice at 300 K, vacancy lattice at 150 K: still falling after 20000
+# sweeps on the GPU) or tens of thousands of sweeps (cutoff 4 at 200 K),
+# which no affordable reference run reaches.  The test checks that every
+# series it compares is stationary.
 EQ_CASES = [
     dict(name="plain", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.0), occupancy=1.0, T=(500, 700, 1000),
          equil=(500, 500, 500)),
-    dict(name="vacfield", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.1), occupancy=0.7, T=(150, 300),
-         equil=(2500, 500)),
-    dict(name="rc4cage", L=32, cutoff=4, cage_strain=0.5, efield=(0.05, 0.0, 0.05), occupancy=0.9, T=(300, 500),
+    dict(name="vacfield", L=32, cutoff=3, cage_strain=1.0, efield=(0.0, 0.0, 0.1), occupancy=0.7, T=(300, 500),
          equil=(500, 500)),
+    dict(name="rc4cage", L=32, cutoff=4, cage_strain=0.5, efield=(0.05, 0.0, 0.05), occupancy=0.9, T=(300, 500),
+         equil=(3000, 500)),
 ]
-EQ_SEEDS = 16
+EQ_SEEDS = 32
 EQ_PROD = 200
 
 

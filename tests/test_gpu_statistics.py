@@ -3,27 +3,30 @@ reference's own random-sequential runs.
 
 tests/golden/ref_equilibrium.npz holds per-sweep E/site and |P|/site of the
 unmodified reference (MT19937, MC_move, src/starrynight-montecarlo-core.c:
-143-191) on 32^3 lattices, 16 independent seeds per temperature, 200
-production sweeps after a per-temperature equilibration of 500 to 3000
-sweeps (tests/golden/make_golden.py), for three Hamiltonians:
+143-191) on 32^3 lattices, 32 independent seeds per temperature, 200
+production sweeps after 500 equilibration sweeps (tests/golden/make_golden.py),
+for three Hamiltonians:
   plain     cutoff 3, CageStrain 1, no field, every site occupied,
-            T in {500, 700, 1000} K (below 500 K this lattice keeps ordering
-            for thousands of sweeps: it has no equilibrium within reach);
+            T in {500, 700, 1000} K;
   vacfield  cutoff 3, CageStrain 1, 30 % vacancies zeroed after
             solid_solution (src/starrynight-lattice.c:139-171), Efield
-            (0, 0, 0.1) (src/starrynight-montecarlo-core.c:120-121), T in
-            {150, 300} K;
+            (0, 0, 0.1) (src/starrynight-montecarlo-core.c:120-121), the
+            physics of the 256^3 benchmark lattice, T in {300, 500} K;
   rc4cage   cutoff 4, CageStrain 0.5, Efield (0.05, 0, 0.05), 10 % vacancies,
-            T in {300, 500} K (at 200 K it keeps relaxing for more than
-            10^4 sweeps on both sides: no equilibrium within reach).
+            T in {300, 500} K.
+At these temperatures E/site is flat after a few hundred sweeps on both
+sides (measured relaxation curves); below them the lattices keep ordering
+for thousands to tens of thousands of sweeps (plain at 300 K, vacfield at
+150 K, rc4cage at 200 K), which no affordable reference run reaches, and a
+comparison there would compare transients of two different dynamics.
 The colour sweep satisfies detailed balance with the same stationary
 distribution, so equilibrium averages -- not trajectories -- must agree, and
-only where both sides are in equilibrium: every compared series must be
-stationary (its second half agrees with its first half within 3 sigma).
+every compared series must be stationary (its second half agrees with its
+first half within 3 sigma).
 
 Error bars: each run (one seed) is one block; the runs are independent, so
 the standard error of a side's mean is the spread of its run means
-(ddof = 1) over sqrt(runs).  The GPU side runs 32 seeds per temperature.
+(ddof = 1) over sqrt(runs).  The GPU side runs 64 seeds per temperature.
 Agreement: |mean_gpu - mean_ref| < 3 sigma_combined, with no added slack."""
 import os
 
@@ -32,7 +35,7 @@ import pytest
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "ref_equilibrium.npz")
 N_SIGMA = 3.0
-GPU_SEEDS = 32
+GPU_SEEDS = 64
 CASES = ("plain", "vacfield", "rc4cage")
 
 
