@@ -417,13 +417,20 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     int *wc = cnt + 8;  // accepted moves per target warp in the current group
     const int nAw = (tg + 31) >> 5;  // target warps
 
-    // this thread's target role: target tt of every colour group.  All
-    // threads stage proposals (thread tid for target tt = tid % tg of groups
-    // pj0, pj0 + NT/tg, ... of a chunk); threads tid < tg also finalize.
-    const int tt = tid % tg, pj0 = tid / tg, pstride = NT / tg;
+    // this thread's target role: target tt = tid % tg of every colour group.
+    // Threads tid < tg decide the group's moves (phase A).  Proposals are
+    // staged by the threads from sb on (thread tid for target tt of groups
+    // pj0, pj0 + pstride, ... of a chunk): when tg is a multiple of 32 and
+    // the other warps can stage a whole group, only they do, while the
+    // target warps run phase A of the chunk's first group (ovl); otherwise
+    // every thread stages at the start of the chunk.
+    const bool ovl = tg % 32 == 0 && NT - tg >= tg;
+    const int sb = ovl ? tg : 0;
+    const int tt = tid % tg, pstride = (NT - sb) / tg, pj0 = (tid - sb) / tg;
+    const bool stager = tid >= sb && tid - sb < pstride * tg;
     const int hh = tt / tp, t = tt - (tt / tp) * tp;
     const int qz = t % nqz, qy = (t / nqz) % nqy, qx = t / (nqz * nqy);
-    const bool tvalid = tid < pstride * tg && qx < Gm.nq[0];
+    const bool tvalid = stager && qx < Gm.nq[0];
     const int trel = (S * qx * T1 + S * qy) * T2 + S * qz;
     const int srel = ((S * qx) * Y + S * qy) * Z + S * qz;
 
@@ -464,7 +471,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     auto stage = [&](int c) {
         const int g0 = c * pc, nk = min(pc, ng - g0);
         float4 *buf = props + (c & 1) * (2 * pc * tg);
-        if (tid < pstride * tg) {
+        if (stager) {
             for (int k = pj0; k < nk; k += pstride) {
                 int cx, cy, cz;
                 group_colour<S, S, MERGE>(g0 + k, hh, cx, cy, cz);
@@ -492,9 +499,13 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         if (g == gnext) {
             c++;
             gnext = g + pc;
-            if (c + 1 < nchunks) stage(c + 1);  // into the buffer chunk c - 1 used (all done with it)
-            else cp_async_commit();
-            cp_async_wait_group<1>();  // the tile and chunk c have landed (chunk c + 1 may be in flight)
+            if (ovl) {
+                cp_async_wait_group<0>();  // the tile and chunk c have landed (chunk c + 1 is staged below)
+            } else {
+                if (c + 1 < nchunks) stage(c + 1);  // into the buffer chunk c - 1 used (all done with it)
+                else cp_async_commit();
+                cp_async_wait_group<1>();  // the tile and chunk c have landed (chunk c + 1 may be in flight)
+            }
             if (g == 0 && a.tile_copy) mbar_wait_bounded(tbar, tphase, a.err);
             if (g == 0 && fill)
                 fill_pairs<RC>(std::make_integer_sequence<int, NP>{}, reinterpret_cast<CPair *>(smem + cv.pairs), tid,
@@ -521,6 +532,9 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
             }
             gchunk = g;
             cur = props + (c & 1) * (2 * pc * tg);
+            // the staging warps issue chunk c + 1 (into the buffer chunk c - 1
+            // used, read before the barrier above) while phase A runs
+            if (ovl && c + 1 < nchunks) stage(c + 1);
         }
 
         // ---- A. targets of the group: dE from the cached field, accept, record ---------
