@@ -778,7 +778,11 @@ __global__ void __launch_bounds__(SN_CACHED_THREADS, 2) gfield_tiled(const SnFie
     cp_async_wait_all();
     __syncthreads();
 
-    double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    // The energy and polarisation sums of the thread's sites as compensated
+    // FP32 sums (FP64 is a slow pipe on this GPU; it is used only to add the
+    // warps' results): 0 p.g (in units of 2^-k), 2 p.E, 3 |px| + |py| (K
+    // term), 4-6 L p, 7-9 p.
+    KahanF acc[10];
     const int nsite = Bx * By * Bz;
     for (int i = tid; i < nsite; i += NT) {
         const int lz = i % Bz, ly = (i / Bz) % By, lx = i / (Bz * By);
@@ -796,21 +800,44 @@ __global__ void __launch_bounds__(SN_CACHED_THREADS, 2) gfield_tiled(const SnFie
         }
         const float px = tp[slot], py = tp[cs + slot], pz = tp[2 * cs + slot];
         const float Li = R.len[site];  // 0 at vacancies, whose dipole is zero
-        acc[0] += 0.5 * ginv * ((double)px * gx + (double)py * gy + (double)pz * gz);
-        acc[2] += (double)px * Ex + (double)py * Ey + (double)pz * Ez;
-        if (Kk > 0.0f && Li != 0.0f) acc[3] -= (double)Kk * (fabs((double)px) + fabs((double)py));
-        acc[4] += (double)Li * px;
-        acc[5] += (double)Li * py;
-        acc[6] += (double)Li * pz;
-        acc[7] += px;
-        acc[8] += py;
-        acc[9] += pz;
+        acc[0].add(fmaf(px, (float)gx, fmaf(py, (float)gy, pz * (float)gz)));
+        acc[2].add(fmaf(px, Ex, fmaf(py, Ey, pz * Ez)));
+        if (Kk > 0.0f && Li != 0.0f) acc[3].add(fabsf(px) + fabsf(py));
+        acc[4].add(Li * px);
+        acc[5].add(Li * py);
+        acc[6].add(Li * pz);
+        acc[7].add(px);
+        acc[8].add(py);
+        acc[9].add(pz);
+    }
+    // warp sums of the (sum, error) pairs by error-free additions (TwoSum)
+    float hs[10], hc[10];
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+        hs[k] = acc[k].s;
+        hc[k] = -acc[k].c;
     }
 #pragma unroll
-    for (int k = 0; k < 10; k++) acc[k] = warp_sum(acc[k]);
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) {
+            if (k == 1) continue;
+            const float bs = __shfl_xor_sync(0xffffffffu, hs[k], o), bc = __shfl_xor_sync(0xffffffffu, hc[k], o);
+            const float t2 = __fadd_rn(hs[k], bs);
+            const float bb = __fsub_rn(t2, hs[k]);
+            const float err = __fadd_rn(__fsub_rn(hs[k], __fsub_rn(t2, bb)), __fsub_rn(bs, bb));
+            hs[k] = t2;
+            hc[k] = __fadd_rn(__fadd_rn(hc[k], bc), err);
+        }
+    }
     if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < 10; k++) red[warp * 16 + k] = acc[k];
+        for (int k = 0; k < 10; k++) {
+            double v = k == 1 ? 0.0 : (double)hs[k] + (double)hc[k];
+            if (k == 0) v *= 0.5 * ginv;
+            else if (k == 3) v *= -(double)Kk;
+            red[warp * 16 + k] = v;
+        }
     }
     __syncthreads();
     if (tid < 10 && a.red) {
