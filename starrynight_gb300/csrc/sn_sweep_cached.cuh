@@ -752,6 +752,134 @@ __device__ __forceinline__ void q_pairs(std::integer_sequence<int, Is...>, const
     (q_pair<RC, MIXED, Is>(tp, cs, slot, T1, T2, w_u, Li, C, scale, ax, ay, az), ...);
 }
 
+// Column form of the pass (cutoffs up to 4): a thread takes 4 consecutive
+// z sites of a row; for each column (ox, oy) of the cutoff disk it loads the
+// column's dipoles around them with 16-byte loads (z from lz0 - 4 to lz0 + 7)
+// and adds every contribution (ox, oy, oz) to each of the 4 sites.  Each
+// contribution is q_pair's, with T_{-o} = T_o, so the integers are the same.
+struct GCol {
+    int x, y, h;  // column offset and the half-height of the cutoff sphere above it
+};
+
+constexpr int gcol_count(int rc)
+{
+    int n = 0;
+    for (int x = -rc; x <= rc; x++)
+        for (int y = -rc; y <= rc; y++)
+            if (x * x + y * y <= rc * rc) n++;
+    return n;
+}
+
+constexpr GCol gcol_at(int rc, int idx)
+{
+    int n = 0;
+    for (int x = -rc; x <= rc; x++)
+        for (int y = -rc; y <= rc; y++)
+            if (x * x + y * y <= rc * rc) {
+                if (n == idx) {
+                    int h = 0;
+                    while ((h + 1) * (h + 1) <= rc * rc - x * x - y * y) h++;
+                    return GCol{x, y, h};
+                }
+                n++;
+            }
+    return GCol{0, 0, 0};
+}
+
+// Contribution of offset (OX, OY, OZ) to the 4 sites from the column's
+// values v[k] at z = lz0 - 4 + k.
+template <bool MIXED, int OX, int OY, int OZ>
+__device__ __forceinline__ void gcell(const float (&vx)[12], const float (&vy)[12], const float (&vz)[12],
+                                      const float (&vl)[12], const float (&Lt)[4], float w_u, float C, float scale,
+                                      uint32_t (&ax)[4], uint32_t (&ay)[4], uint32_t (&az)[4])
+{
+    if constexpr (OX != 0 || OY != 0 || OZ != 0) {
+        constexpr float t0 = (float)sn_stencil::tensor_d(OX, OY, OZ, 0);
+        constexpr float t1 = (float)sn_stencil::tensor_d(OX, OY, OZ, 1);
+        constexpr float t2 = (float)sn_stencil::tensor_d(OX, OY, OZ, 2);
+        constexpr float t3 = (float)sn_stencil::tensor_d(OX, OY, OZ, 3);
+        constexpr float t4 = (float)sn_stencil::tensor_d(OX, OY, OZ, 4);
+        constexpr float t5 = (float)sn_stencil::tensor_d(OX, OY, OZ, 5);
+        constexpr bool NN = OX * OX + OY * OY + OZ * OZ == 1;
+        const bool fold = NN && !MIXED && w_u == 1.0f;
+        const float m0 = fold ? __fsub_rn(t0, C) : t0, m1 = fold ? __fsub_rn(t1, C) : t1,
+                    m2 = fold ? __fsub_rn(t2, C) : t2;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float px = vx[j + OZ + 4], py = vy[j + OZ + 4], pz = vz[j + OZ + 4];
+            const float w = MIXED ? __fmul_rn(Lt[j], vl[j + OZ + 4]) : w_u;
+            float qx = t4 != 0.0f ? __fmul_rn(t4, pz) : 0.0f;
+            if (t3 != 0.0f) qx = fmaf(t3, py, qx);
+            qx = fmaf(m0, px, qx);
+            float qy = t5 != 0.0f ? __fmul_rn(t5, pz) : 0.0f;
+            qy = fmaf(m1, py, qy);
+            if (t3 != 0.0f) qy = fmaf(t3, px, qy);
+            float qz = __fmul_rn(m2, pz);
+            if (t5 != 0.0f) qz = fmaf(t5, py, qz);
+            if (t4 != 0.0f) qz = fmaf(t4, px, qz);
+            if (MIXED || w != 1.0f) {
+                qx = __fmul_rn(w, qx);
+                qy = __fmul_rn(w, qy);
+                qz = __fmul_rn(w, qz);
+            }
+            if (NN && !fold) {
+                qx = __fsub_rn(qx, __fmul_rn(C, px));
+                qy = __fsub_rn(qy, __fmul_rn(C, py));
+                qz = __fsub_rn(qz, __fmul_rn(C, pz));
+            }
+            ax[j] += q_bits(qx, scale);
+            ay[j] += q_bits(qy, scale);
+            az[j] += q_bits(qz, scale);
+        }
+    }
+}
+
+template <bool MIXED, int OX, int OY, int H, int... Ks>
+__device__ __forceinline__ void gcells(std::integer_sequence<int, Ks...>, const float (&vx)[12], const float (&vy)[12],
+                                       const float (&vz)[12], const float (&vl)[12], const float (&Lt)[4], float w_u,
+                                       float C, float scale, uint32_t (&ax)[4], uint32_t (&ay)[4], uint32_t (&az)[4])
+{
+    (gcell<MIXED, OX, OY, Ks - H>(vx, vy, vz, vl, Lt, w_u, C, scale, ax, ay, az), ...);
+}
+
+__device__ __forceinline__ void lds4(float *dst, const float *src)
+{
+    const float4 v = *reinterpret_cast<const float4 *>(src);
+    dst[0] = v.x;
+    dst[1] = v.y;
+    dst[2] = v.z;
+    dst[3] = v.w;
+}
+
+// All contributions of column CI to the 4 sites whose first slot is slot0.
+template <int RC, bool MIXED, int CI>
+__device__ __forceinline__ void gcolumn(const float *__restrict__ tp, int cs, int slot0, int T1, int T2, float w_u,
+                                        const float (&Lt)[4], float C, float scale, uint32_t (&ax)[4],
+                                        uint32_t (&ay)[4], uint32_t (&az)[4])
+{
+    constexpr GCol cl = gcol_at(RC, CI);
+    const int base = slot0 + (cl.x * T1 + cl.y) * T2;
+    float vx[12], vy[12], vz[12], vl[12];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (c != 1 && cl.h == 0) continue;  // a column of one cell per site needs only its own chunk
+        lds4(vx + 4 * c, tp + base + 4 * (c - 1));
+        lds4(vy + 4 * c, tp + cs + base + 4 * (c - 1));
+        lds4(vz + 4 * c, tp + 2 * cs + base + 4 * (c - 1));
+        if (MIXED) lds4(vl + 4 * c, tp + 3 * cs + base + 4 * (c - 1));
+    }
+    gcells<MIXED, cl.x, cl.y, cl.h>(std::make_integer_sequence<int, 2 * cl.h + 1>{}, vx, vy, vz, vl, Lt, w_u, C, scale,
+                                    ax, ay, az);
+}
+
+template <int RC, bool MIXED, int... Cs>
+__device__ __forceinline__ void gcolumns(std::integer_sequence<int, Cs...>, const float *tp, int cs, int slot0, int T1,
+                                         int T2, float w_u, const float (&Lt)[4], float C, float scale,
+                                         uint32_t (&ax)[4], uint32_t (&ay)[4], uint32_t (&az)[4])
+{
+    (gcolumn<RC, MIXED, Cs>(tp, cs, slot0, T1, T2, w_u, Lt, C, scale, ax, ay, az), ...);
+}
+
 template <int RC, bool MIXED>
 __global__ void __launch_bounds__(SN_CACHED_THREADS, 2) gfield_tiled(const SnFieldArgs a)
 {
@@ -783,21 +911,8 @@ __global__ void __launch_bounds__(SN_CACHED_THREADS, 2) gfield_tiled(const SnFie
     // warps' results): 0 p.g (in units of 2^-k), 2 p.E, 3 |px| + |py| (K
     // term), 4-6 L p, 7-9 p.
     KahanF acc[10];
-    const int nsite = Bx * By * Bz;
-    for (int i = tid; i < nsite; i += NT) {
-        const int lz = i % Bz, ly = (i / Bz) % By, lx = i / (Bz * By);
-        const int slot = ((lx + Gm.cH[0]) * T1 + ly + Gm.cH[1]) * T2 + lz + Gm.cH[2];
-        const float Lt = MIXED ? tp[3 * cs + slot] : 0.0f;
-        uint32_t ax = 0u, ay = 0u, az = 0u;
-        q_pairs<RC, MIXED>(std::make_integer_sequence<int, NP>{}, tp, cs, slot, T1, T2, w_u, Lt, C, scale, ax, ay, az);
-        const uint32_t bias = (uint32_t)(2 * NP) * SN_Q_MAGIC_BITS;
-        const int gx = (int)(ax - bias), gy = (int)(ay - bias), gz = (int)(az - bias);
-        const long long site = ((long long)(w.x0 + lx) * Y + (w.y0 + ly)) * Z + w.z0 + lz;
-        if (a.write_g) {
-            R.gcache[site] = gx;
-            R.gcache[N + site] = gy;
-            R.gcache[2 * N + site] = gz;
-        }
+    const uint32_t bias = (uint32_t)(2 * NP) * SN_Q_MAGIC_BITS;
+    auto site_sums = [&](int slot, long long site, int gx, int gy, int gz) {
         const float px = tp[slot], py = tp[cs + slot], pz = tp[2 * cs + slot];
         const float Li = R.len[site];  // 0 at vacancies, whose dipole is zero
         acc[0].add(fmaf(px, (float)gx, fmaf(py, (float)gy, pz * (float)gz)));
@@ -809,6 +924,51 @@ __global__ void __launch_bounds__(SN_CACHED_THREADS, 2) gfield_tiled(const SnFie
         acc[7].add(px);
         acc[8].add(py);
         acc[9].add(pz);
+    };
+    if constexpr (RC <= 4) {
+        // column form: 4 consecutive z sites per thread (Bz, Z and the z halo are multiples of 4)
+        const int nzb = Bz >> 2, ncol = Bx * By * nzb;
+        for (int i = tid; i < ncol; i += NT) {
+            const int lz0 = 4 * (i % nzb), ly = (i / nzb) % By, lx = i / (nzb * By);
+            const int slot0 = ((lx + Gm.cH[0]) * T1 + ly + Gm.cH[1]) * T2 + lz0 + Gm.cH[2];
+            float Lt[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (MIXED) lds4(Lt, tp + 3 * cs + slot0);
+            uint32_t ax[4] = {0u, 0u, 0u, 0u}, ay[4] = {0u, 0u, 0u, 0u}, az[4] = {0u, 0u, 0u, 0u};
+            gcolumns<RC, MIXED>(std::make_integer_sequence<int, gcol_count(RC)>{}, tp, cs, slot0, T1, T2, w_u, Lt, C,
+                                scale, ax, ay, az);
+            int4 gx, gy, gz;
+            gx.x = (int)(ax[0] - bias), gx.y = (int)(ax[1] - bias), gx.z = (int)(ax[2] - bias), gx.w = (int)(ax[3] - bias);
+            gy.x = (int)(ay[0] - bias), gy.y = (int)(ay[1] - bias), gy.z = (int)(ay[2] - bias), gy.w = (int)(ay[3] - bias);
+            gz.x = (int)(az[0] - bias), gz.y = (int)(az[1] - bias), gz.z = (int)(az[2] - bias), gz.w = (int)(az[3] - bias);
+            const long long site0 = ((long long)(w.x0 + lx) * Y + (w.y0 + ly)) * Z + w.z0 + lz0;
+            if (a.write_g) {
+                *reinterpret_cast<int4 *>(R.gcache + site0) = gx;
+                *reinterpret_cast<int4 *>(R.gcache + N + site0) = gy;
+                *reinterpret_cast<int4 *>(R.gcache + 2 * N + site0) = gz;
+            }
+            site_sums(slot0, site0, gx.x, gy.x, gz.x);
+            site_sums(slot0 + 1, site0 + 1, gx.y, gy.y, gz.y);
+            site_sums(slot0 + 2, site0 + 2, gx.z, gy.z, gz.z);
+            site_sums(slot0 + 3, site0 + 3, gx.w, gy.w, gz.w);
+        }
+    } else {
+        const int nsite = Bx * By * Bz;
+        for (int i = tid; i < nsite; i += NT) {
+            const int lz = i % Bz, ly = (i / Bz) % By, lx = i / (Bz * By);
+            const int slot = ((lx + Gm.cH[0]) * T1 + ly + Gm.cH[1]) * T2 + lz + Gm.cH[2];
+            const float Lt = MIXED ? tp[3 * cs + slot] : 0.0f;
+            uint32_t ax = 0u, ay = 0u, az = 0u;
+            q_pairs<RC, MIXED>(std::make_integer_sequence<int, NP>{}, tp, cs, slot, T1, T2, w_u, Lt, C, scale, ax, ay,
+                               az);
+            const int gx = (int)(ax - bias), gy = (int)(ay - bias), gz = (int)(az - bias);
+            const long long site = ((long long)(w.x0 + lx) * Y + (w.y0 + ly)) * Z + w.z0 + lz;
+            if (a.write_g) {
+                R.gcache[site] = gx;
+                R.gcache[N + site] = gy;
+                R.gcache[2 * N + site] = gz;
+            }
+            site_sums(slot, site, gx, gy, gz);
+        }
     }
     // warp sums of the (sum, error) pairs by error-free additions (TwoSum)
     float hs[10], hc[10];
