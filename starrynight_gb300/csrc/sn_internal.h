@@ -25,10 +25,11 @@
 #define SN_ACC_SETS 2
 #endif
 #define SN_SWEEP_MAX_THREADS (SN_TWO_PER_SM_THREADS > 256 ? SN_TWO_PER_SM_THREADS : SN_MAX_THREADS)
-// x slabs of a host upload (each converted and fed to the energy pass as it
-// lands); 8 measured faster than 16 at 256^3 (2.00 vs 2.24 ms).
+// x slabs of a host upload (each converted and fed to the field-cache pass as
+// it lands); at 256^3 an upload took 1.86, 1.74, 1.69 and 1.65 ms with 4, 8,
+// 16 and 32 slabs.
 #ifndef SN_UPLOAD_SLABS
-#define SN_UPLOAD_SLABS 8
+#define SN_UPLOAD_SLABS 32
 #endif
 // streams the upload's energy-pass chunks alternate between (1 or 2)
 #ifndef SN_UPLOAD_FIELD_STREAMS
