@@ -700,7 +700,15 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
     // independent item; a thread runs the whole stencil of its items, so the
     // loop needs no barrier.  Lanes of a warp take consecutive targets of one
     // group, the conflict-free pattern of the tile layout.
+    // Sums 0 (1/2) L p.H, 1 p.nn, 2 p.E, 3 K term, 4-6 L p, 7-9 p: in FP64 for
+    // the FP64 pass; for the FP32 pass compensated FP32 sums per thread
+    // (FP64 is a slow pipe on this GPU), combined by TwoSum within warps.
     double acc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    KahanF facc[10];
+    auto add = [&](int k, R v) {
+        if constexpr (sizeof(R) == 4) facc[k].add(v);
+        else acc[k] += (double)v;
+    };
     const int items = ng * tg;
     for (int it = tid; it < items; it += nthreads) {
         const int g = it / tg, tt = it - (it / tg) * tg;
@@ -773,19 +781,43 @@ __global__ void __launch_bounds__(SN_MAX_THREADS, 1) field_tiled(const SnFieldAr
             a.grad[3 * site + 1] = (float)(gy - Kk * sy);
             a.grad[3 * site + 2] = (float)gz;
         }
-        acc[0] += 0.5 * (double)(Li * pH);
-        acc[1] += (double)pn;
-        acc[2] += (double)pE;
-        acc[3] += (double)kt;
-        acc[4] += (double)(Li * px);
-        acc[5] += (double)(Li * py);
-        acc[6] += (double)(Li * pz);
-        acc[7] += (double)px;
-        acc[8] += (double)py;
-        acc[9] += (double)pz;
+        add(0, Li * pH);  // halved below
+        add(1, pn);
+        add(2, pE);
+        add(3, kt);
+        add(4, Li * px);
+        add(5, Li * py);
+        add(6, Li * pz);
+        add(7, px);
+        add(8, py);
+        add(9, pz);
     }
+    if constexpr (sizeof(R) == 4) {
+        float hs[10], hc[10];
 #pragma unroll
-    for (int k = 0; k < 10; k++) acc[k] = warp_sum(acc[k]);
+        for (int k = 0; k < 10; k++) {
+            hs[k] = facc[k].s;
+            hc[k] = -facc[k].c;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 10; k++) {
+                const float bs = __shfl_xor_sync(0xffffffffu, hs[k], o), bc = __shfl_xor_sync(0xffffffffu, hc[k], o);
+                const float t2 = __fadd_rn(hs[k], bs);
+                const float bb = __fsub_rn(t2, hs[k]);
+                const float err = __fadd_rn(__fsub_rn(hs[k], __fsub_rn(t2, bb)), __fsub_rn(bs, bb));
+                hs[k] = t2;
+                hc[k] = __fadd_rn(__fadd_rn(hc[k], bc), err);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 10; k++) acc[k] = (double)hs[k] + (double)hc[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 10; k++) acc[k] = warp_sum(acc[k]);
+    }
+    acc[0] *= 0.5;
     if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < 10; k++) red[warp * 16 + k] = acc[k];
