@@ -277,27 +277,33 @@ __global__ void __launch_bounds__(SN_PROP_WARPS * 32, 4)
             nq += __popc(m);
         }
         __syncwarp();
-        // 2. draw 0 for the queued sites, 32 at a time; rejected tries to fs/ft
-        for (int b = 0; b < nq; b += 32) {
-            bool rej = false;
-            uint32_t site = 0;
-            float thr = 0.0f;
-            if (b + lane < nq) {
-                site = q[b + lane];
-                float3 p;
-                float u;
-                const bool ok = sn_proposal_first(site, sweep, SN_STREAM_SWEEP, key, dim, constrain, p, u);
-                thr = u > 0.0f ? -logf(u) / beta : INFINITY;
-                if (ok) out[site] = make_float4(p.x, p.y, p.z, thr);
-                rej = !ok;
+        // 2. draw 0 for the queued sites, 64 at a time (two independent draws
+        // per lane, interleaved by the compiler); rejected tries to fs/ft
+        for (int b = 0; b < nq; b += 64) {
+            const bool v1 = b + lane < nq, v2 = b + 32 + lane < nq;
+            const uint32_t s1 = v1 ? q[b + lane] : 0u, s2 = v2 ? q[b + 32 + lane] : 0u;
+            float3 p1, p2;
+            float u1, u2;
+            const bool ok1 = sn_proposal_first(s1, sweep, SN_STREAM_SWEEP, key, dim, constrain, p1, u1);
+            const bool ok2 = sn_proposal_first(s2, sweep, SN_STREAM_SWEEP, key, dim, constrain, p2, u2);
+            const float thr1 = u1 > 0.0f ? -logf(u1) / beta : INFINITY;
+            const float thr2 = u2 > 0.0f ? -logf(u2) / beta : INFINITY;
+            if (v1 && ok1) out[s1] = make_float4(p1.x, p1.y, p1.z, thr1);
+            if (v2 && ok2) out[s2] = make_float4(p2.x, p2.y, p2.z, thr2);
+            const bool r1 = v1 && !ok1, r2 = v2 && !ok2;
+            const unsigned m1 = __ballot_sync(0xffffffffu, r1), m2 = __ballot_sync(0xffffffffu, r2);
+            if (r1) {
+                const int e = nf + __popc(m1 & below);
+                fs[e] = s1;
+                ft[e] = thr1;
             }
-            const unsigned m = __ballot_sync(0xffffffffu, rej);
-            if (rej) {
-                const int e = nf + __popc(m & below);
-                fs[e] = site;
-                ft[e] = thr;
+            nf += __popc(m1);
+            if (r2) {
+                const int e = nf + __popc(m2 & below);
+                fs[e] = s2;
+                ft[e] = thr2;
             }
-            nf += __popc(m);
+            nf += __popc(m2);
         }
         __syncwarp();
         // 3. full rounds of retries
