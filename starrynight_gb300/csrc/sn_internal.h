@@ -36,7 +36,10 @@
 #define SN_UPLOAD_FIELD_STREAMS 2
 #endif
 #define SN_MAX_S 8               // site-colour stride bound (cutoff + 1 <= 7)
-#define SN_CACHED_THREADS 256    // block size of the cached-field sweep kernel
+#ifndef SN_CACHED_THREADS
+#define SN_CACHED_THREADS 256  // block size of the cached-field sweep kernel
+#endif
+#define SN_GFIELD_THREADS 256  // block size of the field-cache pass
 #define SN_BULK_WAIT_LIMIT (1u << 24)  // polls of the tile-copy barrier before an error is recorded
 #define SN_HIST_CAP 4096         // per-replica per-sweep observable log
 

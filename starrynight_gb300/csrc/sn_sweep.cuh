@@ -924,7 +924,7 @@ cudaError_t launch_gfield_rc(bool mixed, const SnFieldArgs &args, int grid, int 
     void (*fn)(const SnFieldArgs) = mixed ? gfield_tiled<RC, true> : gfield_tiled<RC, false>;
     if (cudaError_t e = set_smem_once(once, mixed ? 1 : 0, fn, 0)) return e;
     if (grid <= 0) return cudaSuccess;
-    fn<<<grid, SN_CACHED_THREADS, smem_bytes, st>>>(args);
+    fn<<<grid, SN_GFIELD_THREADS, smem_bytes, st>>>(args);
     return cudaGetLastError();
 }
 

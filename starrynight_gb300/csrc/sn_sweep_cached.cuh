@@ -65,8 +65,8 @@ __host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, 
     o += (uint32_t)((tg + 31) / 32) * 32u * 32u;  // accepted moves of a group: 32 entries per target warp
     c.cnt = o;
     // the tile-copy mbarrier (bytes 8..15), its phase parity (16..19), the
-    // target warps' accepted-move counts (32..63)
-    o += 64u;
+    // target warps' accepted-move counts (from byte 32, one int per warp)
+    o += 32u + sn_align16(4u * (SN_CACHED_THREADS / 32));
     c.total = o;
     return c;
 }
@@ -881,10 +881,10 @@ __device__ __forceinline__ void gcolumns(std::integer_sequence<int, Cs...>, cons
 }
 
 template <int RC, bool MIXED>
-__global__ void __launch_bounds__(SN_CACHED_THREADS, 2) gfield_tiled(const SnFieldArgs a)
+__global__ void __launch_bounds__(SN_GFIELD_THREADS, 2) gfield_tiled(const SnFieldArgs a)
 {
     using G = Geo<RC, false>;
-    constexpr int NP = G::NP, NT = SN_CACHED_THREADS;
+    constexpr int NP = G::NP, NT = SN_GFIELD_THREADS;
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const SnWork w = a.work[blockIdx.x];
@@ -1009,7 +1009,7 @@ __global__ void __launch_bounds__(SN_CACHED_THREADS, 2) gfield_tiled(const SnFie
 
 __host__ __device__ inline int sn_gfield_smem(int cslots, bool mixed)
 {
-    return (int)(sn_align16((mixed ? 4u : 3u) * (uint32_t)cslots * 4u) + (SN_CACHED_THREADS / 32) * 16u * 8u);
+    return (int)(sn_align16((mixed ? 4u : 3u) * (uint32_t)cslots * 4u) + (SN_GFIELD_THREADS / 32) * 16u * 8u);
 }
 
 }  // namespace sn_sweep
