@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <type_traits>
 
 #include "sn_device.cuh"
 

@@ -154,6 +154,12 @@ __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc)
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 
+// v added to the shared-memory word at byte address a (a reduction: no value returned)
+__device__ __forceinline__ void red_shared_add(uint32_t a, uint32_t v)
+{
+    asm volatile("red.shared.add.u32 [%0], %1;\n" ::"r"(a), "r"(v) : "memory");
+}
+
 // ---- TMA bulk copies (the tile_copy = 1 load path) ------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -389,6 +395,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
 
     const CCarve cv = sn_ccarve(cs, tg, pc, NP, MIXED);
     int *tile = reinterpret_cast<int *>(smem + cv.tile);
+    const uint32_t tile_u32 = smem_u32(tile), cs4 = 4u * (uint32_t)cs;
     float *tlen = MIXED ? reinterpret_cast<float *>(smem + cv.tlen) : nullptr;
     float4 *props = reinterpret_cast<float4 *>(smem + cv.props);
     float4 *list = reinterpret_cast<float4 *>(smem + cv.list);
@@ -443,6 +450,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     const float L2 = __fmul_rn(Lu, Lu);
     float Tq[PPT][6];
     int dq[PPT];
+    uint32_t dq4[PPT];  // 4 dq: the byte delta of +o
     bool nnp[PPT], qok[PPT];
 
     CStats own;
@@ -519,6 +527,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                     qok[k] = prole && q < NP;
                     const CPair &P = pairs[qok[k] ? q : 0];
                     dq[k] = (P.o[0] * T1 + P.o[1]) * T2 + P.o[2];
+                    dq4[k] = 4u * (uint32_t)dq[k];
                     nnp[k] = P.nn != 0;
 #pragma unroll
                     for (int e = 0; e < 6; e++) Tq[k][e] = P.t[e];
@@ -590,23 +599,24 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         // ---- B. scatter the accepted moves' field changes into the tile --------------
         // dg_n = Q(c(p')) - Q(c(p)) for n = a +- o (the magic bias cancels).
         // Moves e = pj, pj + GRP, ... of the warps' lists taken in warp order.
-        int n = wc[0];
+        const int c0 = wc[0];
+        int n = c0;
         for (int q = 1; q < nAw; q++) n += wc[q];
-        int lw = 0, lbase = 0, lcnt = wc[0];  // list region of the current move
-        for (int e = pj; e < n && prole; e += GRP) {
-            while (e - lbase >= lcnt) {
-                lbase += lcnt;
-                lcnt = wc[++lw];
-            }
-            const int le = 32 * lw + e - lbase;
-            const float4 en = list[2 * le], eo = list[2 * le + 1];
-            const int sa = __float_as_int(en.x);
+        if constexpr (MIXED) {
+            int lw = 0, lbase = 0, lcnt = c0;  // list region of the current move
+            for (int e = pj; e < n && prole; e += GRP) {
+                while (e - lbase >= lcnt) {
+                    lbase += lcnt;
+                    lcnt = wc[++lw];
+                }
+                const int le = 32 * lw + e - lbase;
+                const float4 en = list[2 * le], eo = list[2 * le + 1];
+                const int sa = __float_as_int(en.x);
 #pragma unroll
-            for (int k = 0; k < PPT; k++) {
-                if (!qok[k]) continue;
-                const int sp = sa + dq[k], sm = sa - dq[k];
-                uint32_t nx, ny, nz, ox, oy, oz;
-                if constexpr (MIXED) {
+                for (int k = 0; k < PPT; k++) {
+                    if (!qok[k]) continue;
+                    const int sp = sa + dq[k], sm = sa - dq[k];
+                    uint32_t nx, ny, nz, ox, oy, oz;
                     const float wp = __fmul_rn(tlen[sp], eo.w), wm = __fmul_rn(tlen[sm], eo.w);
                     q_contrib(Tq[k], nnp[k], wp, C, gscale, en.y, en.z, en.w, nx, ny, nz);
                     q_contrib(Tq[k], nnp[k], wp, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
@@ -618,23 +628,48 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                     atomicAdd(tile + sm, (int)(nx - ox));
                     atomicAdd(tile + cs + sm, (int)(ny - oy));
                     atomicAdd(tile + 2 * cs + sm, (int)(nz - oz));
-                } else {
-                    if (L2 == 1.0f) {
-                        q_contrib<true>(Tq[k], nnp[k], L2, C, gscale, en.y, en.z, en.w, nx, ny, nz);
-                        q_contrib<true>(Tq[k], nnp[k], L2, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
-                    } else {
-                        q_contrib(Tq[k], nnp[k], L2, C, gscale, en.y, en.z, en.w, nx, ny, nz);
-                        q_contrib(Tq[k], nnp[k], L2, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
-                    }
-                    const int ix = (int)(nx - ox), iy = (int)(ny - oy), iz = (int)(nz - oz);
-                    atomicAdd(tile + sp, ix);
-                    atomicAdd(tile + cs + sp, iy);
-                    atomicAdd(tile + 2 * cs + sp, iz);
-                    atomicAdd(tile + sm, ix);
-                    atomicAdd(tile + cs + sm, iy);
-                    atomicAdd(tile + 2 * cs + sm, iz);
                 }
             }
+        } else if (prole) {
+            // uniform lengths: the same contribution for +o and -o, added by
+            // shared-memory reductions at byte addresses (tile word s at
+            // tile_u32 + 4 s, component c at + c * cs4)
+            auto scatter = [&](auto unit) {
+                constexpr bool W1 = decltype(unit)::value;
+                int lw = 0, lbase = 0, lcnt = c0;
+                for (int e = pj; e < n; e += GRP) {
+                    int le;
+                    if (nAw <= 2) {
+                        le = e < c0 ? e : e + 32 - c0;
+                    } else {
+                        while (e - lbase >= lcnt) {
+                            lbase += lcnt;
+                            lcnt = wc[++lw];
+                        }
+                        le = 32 * lw + e - lbase;
+                    }
+                    const float4 en = list[2 * le], eo = list[2 * le + 1];
+                    const uint32_t at = tile_u32 + 4u * (uint32_t)__float_as_int(en.x);
+#pragma unroll
+                    for (int k = 0; k < PPT; k++) {
+                        if (!qok[k]) continue;
+                        uint32_t nx, ny, nz, ox, oy, oz;
+                        // W1: the cage strain is folded into Tq (nnp false)
+                        q_contrib<W1>(Tq[k], W1 ? false : nnp[k], L2, C, gscale, en.y, en.z, en.w, nx, ny, nz);
+                        q_contrib<W1>(Tq[k], W1 ? false : nnp[k], L2, C, gscale, eo.x, eo.y, eo.z, ox, oy, oz);
+                        const uint32_t ix = nx - ox, iy = ny - oy, iz = nz - oz;
+                        const uint32_t ap = at + dq4[k], am = at - dq4[k];
+                        red_shared_add(ap, ix);
+                        red_shared_add(ap + cs4, iy);
+                        red_shared_add(ap + 2u * cs4, iz);
+                        red_shared_add(am, ix);
+                        red_shared_add(am + cs4, iy);
+                        red_shared_add(am + 2u * cs4, iz);
+                    }
+                }
+            };
+            if (L2 == 1.0f) scatter(std::true_type{});
+            else scatter(std::false_type{});
         }
         __syncthreads();
     }
