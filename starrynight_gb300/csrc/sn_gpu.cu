@@ -314,8 +314,8 @@ bool plan_cached(SnTile &t, int Z, int rc, bool mixed, int limit, int pc_min)
     t.cslots = t.cT[0] * t.cT[1] * t.cT[2];
     // proposal chunks (two buffered): up to 8 groups each, as many as fit
     t.cpc = std::min(t.ng, 8);
-    while (t.cpc > 1 && k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed) > limit) t.cpc--;
-    t.csmem = k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed);
+    while (t.cpc > 1 && k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed, t.ng) > limit) t.cpc--;
+    t.csmem = k_cached_smem[rc](t.cslots, t.tg, t.cpc, mixed, t.ng);
     if (t.csmem > limit || t.cpc < pc_min) return false;
     if (sn_sweep::sn_gfield_smem(t.cslots, mixed) > kSmemLimit) return false;
     t.cmode = 1;

@@ -20,14 +20,14 @@ typedef cudaError_t (*sn_field_launch_fn)(bool fp64, bool two_d, bool mixed, con
 typedef void (*sn_geo_fn)(bool two_d, int *S, int *SZ, int *NS, int *NF, int *merge);
 typedef cudaError_t (*sn_flow_launch_fn)(bool two_d, bool mixed, bool cached, const SnFlowArgs &a, int grid,
                                          int threads, int smem, cudaStream_t st, int *max_grid);
-typedef int (*sn_cached_smem_fn)(int cslots, int tg, int pc, bool mixed);
+typedef int (*sn_cached_smem_fn)(int cslots, int tg, int pc, bool mixed, int ng);
 typedef cudaError_t (*sn_gfield_launch_fn)(bool mixed, const void *field_args, int grid, int smem, cudaStream_t st);
 
 #define SN_DECLARE_RC(N)                                                                                     \
     cudaError_t sn_launch_sweep_rc##N(bool, bool, bool, const SnPhaseArgs &, int, int, int, cudaStream_t);  \
     cudaError_t sn_launch_flow_rc##N(bool, bool, bool, const SnFlowArgs &, int, int, int, cudaStream_t,     \
                                      int *);                                                               \
-    int sn_cached_smem_rc##N(int, int, int, bool);                                                         \
+    int sn_cached_smem_rc##N(int, int, int, bool, int);                                                         \
     cudaError_t sn_launch_gfield_rc##N(bool, const void *, int, int, cudaStream_t);                        \
     cudaError_t sn_launch_field_rc##N(bool, bool, bool, const void *, int, int, int, cudaStream_t);        \
     cudaError_t sn_launch_field64_rc##N(bool, bool, const void *, int, int, int, cudaStream_t);            \

@@ -41,10 +41,10 @@ namespace sn_sweep {
 
 // Shared-memory carve-up of the cached sweep, identical on host and device.
 struct CCarve {
-    uint32_t tile, tlen, props, list, pairs, cnt, red, total;
+    uint32_t tile, tlen, props, list, ctab, pairs, cnt, red, total;
 };
 
-__host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, bool mixed)
+__host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, bool mixed, int ng)
 {
     CCarve c;
     uint32_t o = 0;
@@ -63,6 +63,8 @@ __host__ __device__ inline CCarve sn_ccarve(int cslots, int tg, int pc, int np, 
     o += (uint32_t)(2 * pc * tg) * 32u;  // two chunks of (p', threshold), (p_old, -) per target
     c.list = o;
     o += (uint32_t)((tg + 31) / 32) * 32u * 32u;  // accepted moves of a group: 32 entries per target warp
+    c.ctab = o;
+    o += sn_align16((uint32_t)ng * 16u);  // per group and merged half: tile-slot and site offsets of its colour
     c.cnt = o;
     // the tile-copy mbarrier (bytes 8..15), its phase parity (16..19), the
     // target warps' accepted-move counts (from byte 32, one int per warp)
@@ -393,7 +395,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     const int cH0 = Gm.cH[0], cH1 = Gm.cH[1], cH2 = Gm.cH[2];
     float4 *__restrict__ gprop = R.prop;
 
-    const CCarve cv = sn_ccarve(cs, tg, pc, NP, MIXED);
+    const CCarve cv = sn_ccarve(cs, tg, pc, NP, MIXED, ng);
     int *tile = reinterpret_cast<int *>(smem + cv.tile);
     const uint32_t tile_u32 = smem_u32(tile), cs4 = 4u * (uint32_t)cs;
     float *tlen = MIXED ? reinterpret_cast<float *>(smem + cv.tlen) : nullptr;
@@ -440,6 +442,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     const bool tvalid = stager && qx < Gm.nq[0];
     const int trel = (S * qx * T1 + S * qy) * T2 + S * qz;
     const int srel = ((S * qx) * Y + S * qy) * Z + S * qz;
+    const int sbase = (w.x0 * Y + w.y0) * Z + w.z0 + srel;  // this thread's target site less its colour offset
 
     // this thread's scatter role (phase B): stencil pairs q = pq + k * NT of
     // the accepted moves e = pj, pj + GRP, ...; the pair's tensor T_o, whether
@@ -500,6 +503,15 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         }
         cp_async_commit();
     };
+    // the colour offsets of every group's two halves: tile slot
+    // ((cx + cH0) T1 + cy + cH1) T2 + cz + cH2 and site (cx Y + cy) Z + cz
+    // (read by phase A after the first chunk's barrier)
+    int2 *ctab = reinterpret_cast<int2 *>(smem + cv.ctab);
+    for (int i = tid; i < 2 * ng; i += NT) {
+        int cx, cy, cz;
+        group_colour<S, S, MERGE>(i >> 1, i & 1, cx, cy, cz);
+        ctab[i] = make_int2(((cx + cH0) * T1 + (cy + cH1)) * T2 + cz + cH2, (cx * Y + cy) * Z + cz);
+    }
     stage(0);
     const float4 *cur = props;
     int gchunk = 0, c = -1, gnext = 0;  // chunk of the current group, first group of the next chunk
@@ -555,11 +567,10 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
             int tslot = 0;
             float4 pr = make_float4(0.0f, 0.0f, 0.0f, -2.0f), po = pr;
             if (tid < tg) {
-                int cx, cy, cz;
-                group_colour<S, S, MERGE>(g, hh, cx, cy, cz);
+                const int2 co = ctab[2 * g + hh];
                 pr = cur[2 * ((g - gchunk) * tg + tt)];
                 po = cur[2 * ((g - gchunk) * tg + tt) + 1];
-                tslot = ((cx + cH0) * T1 + (cy + cH1)) * T2 + cz + cH2 + trel;
+                tslot = co.x + trel;
                 if (pr.w >= 0.0f) {
                     const float gx = fmaf((float)tile[tslot], ginv, Ex);
                     const float gy = fmaf((float)tile[cs + tslot], ginv, Ey);
@@ -572,7 +583,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                     st.att++;
                     if (dE < pr.w) {
                         acc = true;
-                        const int site = ((w.x0 + cx) * Y + (w.y0 + cy)) * Z + w.z0 + cz + srel;
+                        const int site = sbase + co.y;
                         gpx[site] = pr.x;
                         gpy[site] = pr.y;
                         gpz[site] = pr.z;
@@ -589,7 +600,9 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
             const unsigned m = __ballot_sync(0xffffffffu, acc);
             if (acc) {
                 const int e = 32 * warp + __popc(m & ((1u << lane) - 1u));
-                list[2 * e] = make_float4(__int_as_float(tslot), pr.x, pr.y, pr.z);
+                // the target's tile slot (mixed lengths) or its byte address in shared memory
+                list[2 * e] = make_float4(__int_as_float(MIXED ? tslot : (int)(tile_u32 + 4u * (uint32_t)tslot)), pr.x,
+                                          pr.y, pr.z);
                 list[2 * e + 1] = make_float4(po.x, po.y, po.z, Li);
             }
             if (lane == 0) wc[warp] = __popc(m);
@@ -649,7 +662,7 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
                         le = 32 * lw + e - lbase;
                     }
                     const float4 en = list[2 * le], eo = list[2 * le + 1];
-                    const uint32_t at = tile_u32 + 4u * (uint32_t)__float_as_int(en.x);
+                    const uint32_t at = __float_as_uint(en.x);
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
                         if (!qok[k]) continue;

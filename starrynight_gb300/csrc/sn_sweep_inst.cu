@@ -31,9 +31,9 @@ cudaError_t SN_CAT(sn_launch_flow_rc, SN_RC)(bool two_d, bool mixed, bool cached
     return sn_sweep::launch_flow_rc<SN_RC>(two_d, mixed, cached, a, grid, threads, smem, st, max_grid);
 }
 
-int SN_CAT(sn_cached_smem_rc, SN_RC)(int cslots, int tg, int pc, bool mixed)
+int SN_CAT(sn_cached_smem_rc, SN_RC)(int cslots, int tg, int pc, bool mixed, int ng)
 {
-    return (int)sn_sweep::sn_ccarve(cslots, tg, pc, sn_sweep::Geo<SN_RC, false>::NP, mixed).total;
+    return (int)sn_sweep::sn_ccarve(cslots, tg, pc, sn_sweep::Geo<SN_RC, false>::NP, mixed, ng).total;
 }
 
 void SN_CAT(sn_geo_rc, SN_RC)(bool two_d, int *S, int *SZ, int *NS, int *NF, int *merge)
