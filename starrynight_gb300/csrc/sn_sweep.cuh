@@ -642,15 +642,20 @@ __global__ void __launch_bounds__(SweepBounds<CACHED>::threads, SweepBounds<CACH
                 cur_rep = rep;
             }
         }
+        // Ordering: the waiting threads' acquire loads of the dependencies'
+        // flags, then the barrier, make the producers' writes visible to
+        // every thread's later loads.  The cached sweep reads other blocks'
+        // data only through L2 (its tile by cp.async.cg, or by TMA after
+        // fence.proxy.async); the stencil sweep stages neighbours' dipoles
+        // through L1 (cp.async.ca), so each of its threads also fences.
+        // After the block, the barrier and thread 0's release store publish
+        // the whole CTA's writes (release is cumulative over the barrier).
         __syncthreads();
-        __threadfence();
+        if constexpr (!CACHED) __threadfence();
         sweep_block_any<RC, TWO_D, MIXED, CACHED, true>(f.base.work[item], f.base, smem, first, &st);
         first = false;
         __syncthreads();
-        if (tid == 0) {
-            __threadfence();
-            st_release_gpu(f.done + item, epoch);
-        }
+        if (tid == 0) st_release_gpu(f.done + item, epoch);
         if (!reserve && tid == 0) s_item = (int)atomicAdd(f.queue, 1u);
         __syncthreads();
         item = s_item;
