@@ -16,8 +16,9 @@
 // fixed-point grid of 2^-k on its own, Q(c_ij) with c_ij = w (T_o p_j) -
 // CageStrain [|o| = 1] p_j, w = len_i len_j (for unit uniform lengths
 // c_ij = (T_o - CageStrain [|o| = 1] I) p_j, the cage strain folded into the
-// tensor), and g_i is the int32 sum of those integers.  A move of site a from p to p' then changes g_n by exactly
-// Q(c(p')) - Q(c(p)), which the sweep adds with integer atomics: integer
+// tensor), and g_i is the int32 sum of those integers.  A move of site a
+// from p to p' then changes g_n by exactly Q(c(p')) - Q(c(p)), which the
+// sweep adds with integer shared-memory atomics or reductions: integer
 // addition is associative, so g after any sequence of moves equals, bit for
 // bit, the g that the field pass (gfield_tiled) computes from scratch for
 // the current lattice -- independent of thread order, schedule, batching or
