@@ -1056,7 +1056,9 @@ sn_status sn_check_flow(const sn_params *params, int n_replicas, const sn_replic
                     }
             std::sort(want.begin(), want.end());
             want.erase(std::unique(want.begin(), want.end()), want.end());
-            std::vector<int> got(dl + 1, dl + 1 + dl[0]);
+            std::vector<int> got;
+            got.reserve((size_t)dl[0]);
+            for (int k = 1; k <= dl[0]; k++) got.push_back(dl[k]);
             std::sort(got.begin(), got.end());
             if (got != want) return fail(nullptr, SN_ERR_SCHEDULE, "item %d: dependency list differs", i);
             for (int j : got)

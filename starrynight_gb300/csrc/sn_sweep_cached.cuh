@@ -383,7 +383,6 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
     float *__restrict__ gpx = R.px;
     float *__restrict__ gpy = R.py;
     float *__restrict__ gpz = R.pz;
-    const float *__restrict__ glen = R.len;
     const int Bx = Gm.B[0], By = Gm.B[1], Bz = Gm.B[2];
     const int T1 = Gm.cT[1], T2 = Gm.cT[2];
     const int tp = Gm.tp, tg = Gm.tg, ng = Gm.ng, pc = Gm.cpc;
