@@ -43,6 +43,17 @@ def test_planner_fits_shared_memory(native_lib, X, Y, Z, rc):
     assert min(s["bx"], s["by"]) >= rc and (Z == 1 or s["bz"] >= rc)
 
 
+def test_headline_plan_keeps_two_ctas_per_sm(native_lib):
+    """The 256^3 cutoff-3 lattice gets the cached-field sweep on 8x8x32 blocks
+    with at most half of the SM's 228 KB of shared memory (less 1 KB reserved
+    per CTA and the kernel's static slots) per CTA: two CTAs per SM, the
+    occupancy the kernel is tuned for."""
+    s = sn.plan_schedule(256, 256, 256, 3)
+    assert s["field_cache"] == 1
+    assert (s["bx"], s["by"], s["bz"]) == (8, 8, 32)
+    assert s["smem_bytes"] <= (228 * 1024 - 2 * 1024) // 2 - 128
+
+
 @pytest.mark.parametrize("X,Y,Z,rc", [(8, 8, 8, 3), (6, 6, 6, 3), (12, 12, 12, 3), (32, 32, 32, 3), (24, 24, 1, 3),
                                       (16, 16, 16, 4), (20, 20, 20, 5), (48, 36, 1, 5), (8, 12, 16, 2), (20, 20, 28, 3)])
 def test_schedule_colours_never_interact(native_lib, X, Y, Z, rc):
