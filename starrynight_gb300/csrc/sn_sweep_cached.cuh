@@ -646,7 +646,8 @@ __device__ __forceinline__ void sweep_block_cached(const SnWork w, const SnPhase
         } else if (prole) {
             // uniform lengths: the same contribution for +o and -o, added by
             // shared-memory reductions at byte addresses (tile word s at
-            // tile_u32 + 4 s, component c at + c * cs4)
+            // tile_u32 + 4 s, component c at + c * cs4; a move's list entry
+            // carries its target's address)
             auto scatter = [&](auto unit) {
                 constexpr bool W1 = decltype(unit)::value;
                 int lw = 0, lbase = 0, lcnt = c0;
