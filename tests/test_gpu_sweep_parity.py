@@ -47,6 +47,8 @@ CACHED_CASES = [
     ("c_constrain_x", (16, 16, 16), 3, 300.0, (0.2, 0, 0), 0.0, 1.0, (1.0,), (1.0,), True, 3, 3),
     ("c_circle_dim2", (16, 16, 16), 3, 300.0, (0, 0, 0), 0.0, 1.0, (1.0,), (1.0,), False, 2, 3),
     ("c_mixture", (16, 16, 16), 3, 300.0, (0, 0, 0.1), 0.0, 1.0, (1.0, 0.5, 0.0), (0.5, 0.3, 0.2), False, 3, 3),
+    ("c_rc4_mixture", (16, 16, 16), 4, 300.0, (0.05, 0.0, 0.05), 0.0, 0.5, (1.0, 0.5, 0.0), (0.5, 0.3, 0.2), False, 3,
+     2),
     ("c_length2", (16, 16, 16), 3, 300.0, (0, 0, 0), 0.0, 1.0, (2.0,), (1.0,), False, 3, 3),
     ("c_rc1", (8, 12, 8), 1, 300.0, (0.0, 0.1, 0.0), 0.0, 1.0, (1.0, 0.0), (0.8, 0.2), False, 3, 3),
 ]
